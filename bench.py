@@ -1,0 +1,334 @@
+#!/usr/bin/env python
+"""Benchmark of the reweighting path: LLH evaluations per second.
+
+Default workload: the 5M-event mixed-dial configuration (8 samples, 3000
+bins, 200 correlated parameters, Barlow-Beeston likelihood), dial math and
+weight products in FP32 with bin sums / sum of w^2 / likelihood in FP64,
+K = 64 parameter points per pass.  One step is one pass over all events for
+the K points.  The dial payload (~2.7 GB) is larger than L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun each rank evaluates its own replica (the path shards by
+events; this build runs replicas only) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "LLH evals/s (5M events, C2 mixed dials)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gw", choices=["gw", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--events", type=int, default=0)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--points", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-variants", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gw" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def llh_type_for(cfg):
+    from gundam_gb300 import _native as N
+
+    return N.GW_LLH_BARLOW_BEESTON_OA2021 if cfg in ("c2", "c5") else N.GW_LLH_POISSON
+
+
+def cpu_baseline(wl, cfg, seconds, threads=None):
+    """The CPU propagation (oracle port) timed on this host: full evaluations, K=1."""
+    from oracle.oracle import Oracle
+
+    threads = threads or (os.cpu_count() or 1)
+    orc = Oracle(wl, llh_type=llh_type_for(cfg))
+    p = wl.nominal()
+    orc.eval(p, threads=threads)  # warm caches
+    t0 = time.perf_counter()
+    orc.eval(p, threads=threads)
+    one = time.perf_counter() - t0
+    n = max(1, min(200, int(seconds / max(one, 1e-6))))
+    pts = wl.draw_points(n, 4242)
+    t0 = time.perf_counter()
+    for i in range(n):
+        orc.eval(pts[i:i + 1], threads=threads)
+    dt = time.perf_counter() - t0
+    orc.close()
+    return n / dt, threads, n, dt
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    from gundam_gb300 import Workload
+
+    wl = Workload(args.config, n_events=args.events, seed=args.seed)
+    from oracle.oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    orc = Oracle(wl, llh_type=llh_type_for(args.config))
+    pts = wl.draw_points(args.warmup + args.steps, 77)
+    for i in range(args.warmup):
+        orc.eval(pts[i:i + 1], threads=threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        orc.eval(pts[args.warmup + i:args.warmup + i + 1], threads=threads)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.config}: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, "
+                               f"{wl.n_params} params", "points_per_step": 1, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full evaluations of all {wl.n_events} events"},
+        "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_device(eng, torch, d, K, steps, warmup, dist):
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        eng.eval_device(d["p"].data_ptr(), K, d["s"].data_ptr(), d["s2"].data_ptr(), d["l"].data_ptr(), 0, sp)
+    torch.cuda.synchronize()
+    eng.sync()
+    eng.set_profiling(True)
+    eng.read_profile()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        eng.eval_device(d["p"].data_ptr(), K, d["s"].data_ptr(), d["s2"].data_ptr(), d["l"].data_ptr(), 0, sp)
+    b.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = a.elapsed_time(b) / steps
+    kms, klaunch, launches = eng.read_profile()
+    eng.set_profiling(False)
+    eng.sync()
+    return ms, kms / max(1, klaunch), launches
+
+
+def run_gw(args, world, rank, local, dist):
+    import numpy as np
+    import torch
+
+    from gundam_gb300 import Engine, Workload
+    from gundam_gb300.roofline import algorithmic_bytes
+
+    torch.cuda.set_device(local)
+    wl = Workload(args.config, n_events=args.events, seed=args.seed)
+    K = args.points
+    eng = Engine.from_workload(wl, precision=args.precision, k_max=max(K, 1), llh_type=llh_type_for(args.config),
+                               device=local)
+    if K > 1:
+        eng.autotune(K)
+    pts = wl.draw_points(K, 1234 + rank)
+    d = {"p": torch.from_numpy(pts).cuda(), "s": torch.empty((K, wl.n_bins), dtype=torch.float64, device="cuda")}
+    d["s2"] = torch.empty_like(d["s"])
+    d["l"] = torch.empty(K, dtype=torch.float64, device="cuda")
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, kernel_ms, launches = time_device(eng, torch, d, K, args.steps, args.warmup, dist)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * K / (ms / 1e3)
+
+    # e2e through the public API with host buffers (params H2D, bins + LLH D2H each step)
+    for _ in range(2):
+        eng.eval(pts)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.eval(pts)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * K / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": K * wl.n_params * 8,
+           "d2h_bytes_per_step": K * wl.n_bins * 16 + K * 16, "ms_per_step": e2e_s * 1e3}
+
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(wl, args.precision, K)
+    achieved = alg / (kernel_ms / 1e3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        tr = json.loads(tfile.read_text())
+        key = f"{args.config}/{args.precision}/K{K}"
+        if key in tr:
+            traffic = tr[key]
+    layout = eng.layout()
+    variants = {}
+    if not args.no_variants:
+        # the same engine at K=1 (plain kernel), and the FP64 engine at K=1
+        ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
+        variants[f"{args.precision}_K1"] = {
+            "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
+            "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9}
+        if args.precision == "fp32":
+            eng.close()
+            eng = Engine.from_workload(wl, precision="fp64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
+                                       device=local)
+            ms64, kms64, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
+            variants["fp64_K1"] = {
+                "evals_per_s": 1e3 / ms64, "ms_per_eval": ms64, "kernel_ms": kms64,
+                "kernel_gbs": algorithmic_bytes(wl, "fp64", 1) / (kms64 / 1e3) / 1e9}
+            if K > 1:
+                eng.autotune(K)
+                msk, kmsk, _ = time_device(eng, torch, d, K, args.steps, args.warmup, dist)
+                variants[f"fp64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk}
+        eng.sync()
+    eng.close()
+
+    cpu = None
+    if rank == 0:
+        v, cores, n, dt = cpu_baseline(wl, args.config, args.cpu_seconds)
+        cpu = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+               "sample": f"{n} full evaluations (K=1) of all {wl.n_events} events, {dt:.1f} s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 dials / f64 sums" if args.precision == "fp32" else "f64",
+            "data": "synthetic (seeded generator, C2 shapes)",
+            "config": {"workload": f"{args.config}: {wl.n_events} events, {wl.n_dials} dials, "
+                                   f"{wl.n_bins} bins, {wl.n_params} params",
+                       "points_per_step": K, "precision": args.precision, "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}", "tiles": layout["n_tiles"],
+                       "payload_bytes": layout["payload_bytes"]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_batched" if K > 1 else "k_plain", "kernel_ms": kernel_ms,
+                         "algorithmic_bytes_per_launch": alg},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "variants": variants,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, dist)
+        else:
+            run_gw(args, world, rank, local, dist)
+    finally:
+        if dist is not None and dist.is_initialized():
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

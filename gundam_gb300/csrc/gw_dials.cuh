@@ -1,0 +1,258 @@
+// gw_dials.cuh -- per-dial response functions evaluated on the device.
+//
+// Each function restates the arithmetic of the reference's shared CPU/GPU
+// headers in src/Utils/include/Calculate*.h, in the same operation order, for
+// T = double (FP64 mode) or T = float (FP32 mode).  Data is read from the tile
+// payload in shared memory.  The CPU dial wrappers call these with bounds
+// (-1e20, 1e20) and apply the collection's response clamp afterwards
+// (MonotonicSpline.cpp:71-84, DialResponseSupervisor.cpp:10-18); the engine
+// does the same.
+#pragma once
+#include "gw_layout.h"
+
+namespace gw {
+
+template <typename T>
+__device__ __forceinline__ T clamp_bounds(T v) {
+  const T lo = T(-1e20), hi = T(1e20);
+  if (v < lo) v = lo;
+  if (v > hi) v = hi;
+  return v;
+}
+
+// Hermite cubic on [p1, p2] with end slopes m1, m2 (already scaled by the
+// interval width), Horner form of CalculateUniformSpline.h:71-74.
+template <typename T>
+__device__ __forceinline__ T hermite(T p1, T m1, T p2, T m2, T fx) {
+  return ((((T(2) * p1 - T(2) * p2 + m2 + m1) * fx + T(3) * p2 - T(3) * p1 - m2 - T(2) * m1) * fx +
+           m1) * fx + p1);
+}
+
+// Catmull-Rom spline on uniform knots, with (limit == true) the
+// Fritsch-Carlson slope limiter: CalculateMonotonicSpline.h:49-148 and
+// (limit == false) CalculateCompactSpline.h:48-126.
+// d = [low, step, y_0 .. y_{n-1}].
+template <typename T, bool limit>
+__device__ __forceinline__ T eval_catmull(const T* __restrict__ d, int n, T x, bool trunc) {
+  const T low = d[0];
+  const T step = d[1];
+  if (trunc) {  // MonotonicSpline.cpp:78-81
+    const T high = low + T(n - 1) * step;
+    if (x <= low) x = low;
+    else if (x >= high) x = high;
+  }
+  const T xx = (x - low) / step;
+  const int ix = (xx < T(0)) ? (int)(xx - T(1)) : (int)xx;
+  const int last = n - 2;
+  const int a = min(max(ix - 1, 0), last);
+  const int b = min(max(ix, 0), last);
+  const int c = min(max(ix + 1, 0), last);
+  const T* y = d + 2;
+  const T p2 = y[b];
+  const T p3 = y[b + 1];
+  const T fx = xx - T(b);
+  const T d21 = y[a + 1] - y[a];
+  const T d32 = p3 - p2;
+  const T d43 = y[c + 1] - y[c];
+  T m2 = T(0.5) * (d21 + d32);
+  T m3 = T(0.5) * (d32 + d43);
+  if (limit) {
+    if (d32 * d21 <= T(0)) m2 = T(0);
+    if (d43 * d32 <= T(0)) m3 = T(0);
+    const T ad21 = (d21 < T(0)) ? -d21 : d21;
+    const T ad32 = (d32 < T(0)) ? -d32 : d32;
+    const T ad43 = (d43 < T(0)) ? -d43 : d43;
+    const T delta2 = T(3) * ((ad21 < ad32) ? ad21 : ad32);
+    const T delta3 = T(3) * ((ad32 < ad43) ? ad32 : ad43);
+    if (m2 > delta2) m2 = delta2;
+    if (m2 < -delta2) m2 = -delta2;
+    if (m3 > delta3) m3 = delta3;
+    if (m3 < -delta3) m3 = -delta3;
+  }
+  const T v = ((((T(2) * p2 - T(2) * p3 + m3 + m2) * fx + T(3) * p3 - T(3) * p2 - m3 - T(2) * m2) * fx +
+                m2) * fx + p2);
+  return clamp_bounds(v);
+}
+
+// Hermite spline on uniform knots with stored slopes: CalculateUniformSpline.h:46-80.
+// d = [low, step, (y, dydx) x n].
+template <typename T>
+__device__ __forceinline__ T eval_uniform(const T* __restrict__ d, int n, T x, bool trunc) {
+  const T low = d[0];
+  const T step = d[1];
+  if (trunc) {  // UniformSpline.cpp:47-60
+    const T high = low + T(n - 1) * step;
+    if (x <= low) x = low;
+    else if (x >= high) x = high;
+  }
+  const T xx = (x - low) / step;
+  int ix = (int)xx;
+  if (ix < 0) ix = 0;
+  if (ix > n - 2) ix = n - 2;  // same interval choice as "2*ix+7>dim"
+  const T fx = xx - T(ix);
+  const T* k = d + 2 + 2 * ix;
+  const T p1 = k[0];
+  const T m1 = k[1] * step;
+  const T p2 = k[2];
+  const T m2 = k[3] * step;
+  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
+}
+
+// Hermite spline on non-uniform knots: CalculateGeneralSpline.h:51-197, with
+// its 5-step branch-free search (:135-159).  Here the payload drops the unused
+// [low, step] prefix: d = [(y, dydx, x) x n].
+template <typename T>
+__device__ __forceinline__ T eval_general(const T* __restrict__ d, int n, T x, bool trunc) {
+  if (trunc) {  // GeneralSpline.cpp:33-42
+    const T lo = d[2];
+    const T hi = d[3 * (n - 1) + 2];
+    if (x <= lo) x = lo;
+    else if (x >= hi) x = hi;
+  }
+  const int kc = n - 1;
+  int ix = 0;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    if ((ix + off < kc) && (x > d[3 * (ix + off) + 2])) ix += off;
+  }
+  const T x1 = d[3 * ix + 2];
+  const T x2 = d[3 * (ix + 1) + 2];
+  const T step = x2 - x1;
+  const T fx = (x - x1) / step;
+  const T p1 = d[3 * ix];
+  const T m1 = d[3 * ix + 1] * step;
+  const T p2 = d[3 * (ix + 1)];
+  const T m2 = d[3 * (ix + 1) + 1] * step;
+  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
+}
+
+// Piecewise-linear graph: CalculateGraph.h:43-88.  d = [(y, x) x n].
+template <typename T>
+__device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, bool trunc) {
+  if (n < 2) return d[0];
+  if (trunc) {  // Graph.cpp:47-51 returns the end values directly
+    if (x <= d[1]) return d[0];
+    if (x >= d[2 * n - 1]) return d[2 * n - 2];
+  }
+  int ix = 0;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    if ((ix + off < n) && (x > d[2 * (ix + off) + 1])) ix += off;
+  }
+  if (ix + 1 >= n) ix--;
+  const T p1 = d[2 * ix];
+  const T x1 = d[2 * ix + 1];
+  const T p2 = d[2 * (ix + 1)];
+  const T x2 = d[2 * (ix + 1) + 1];
+  const T step = x2 - x1;
+  const T fx = (x - x1) / step;
+  const T m = p2 - p1;
+  return clamp_bounds(p1 + fx * m);
+}
+
+// Index of the facet for a value: BilinearIndex / BicubicIndex
+// (CalculateBilinearInterpolation.h:36-60), restricted to in-range reads.
+template <typename T>
+__device__ __forceinline__ int surface_index(T v, const T* __restrict__ a, int na) {
+  int i = 0;
+  if (8 < na && !(v < a[8])) i = 8;
+  if ((i + 4) < na && !(v < a[i + 4])) i += 4;
+  if ((i + 2) < na && !(v < a[i + 2])) i += 2;
+  if ((i + 1) < na && !(v < a[i + 1])) i += 1;
+  return i;
+}
+
+template <typename T>
+__device__ __forceinline__ T lin(T x, T x0, T p0, T x1, T p1) {
+  return p0 + (p1 - p0) * (x - x0) / (x1 - x0);
+}
+
+// Bilinear surface: CalculateBilinearInterpolation.h:103-152.
+// d = [nx, ny, xx[nx], yy[ny], z[nx*ny]] (z index = ix*ny + iy).
+template <typename T>
+__device__ __forceinline__ T eval_bilinear(const T* __restrict__ d, T x, T y, bool trunc) {
+  const int nx = (int)d[0];
+  const int ny = (int)d[1];
+  const T* xx = d + 2;
+  const T* yy = xx + nx;
+  const T* z = yy + ny;
+  if (trunc) {  // Bilinear.cpp:40-64
+    if (x < xx[0]) x = xx[0];
+    if (x > xx[nx - 1]) x = xx[nx - 1];
+    if (y < yy[0]) y = yy[0];
+    if (y > yy[ny - 1]) y = yy[ny - 1];
+  }
+  const int ix = surface_index(x, xx, nx - 1);
+  const int iy = surface_index(y, yy, ny - 1);
+  const T v0 = lin(x, xx[ix], z[ix * ny + iy], xx[ix + 1], z[(ix + 1) * ny + iy]);
+  const T v1 = lin(x, xx[ix], z[ix * ny + iy + 1], xx[ix + 1], z[(ix + 1) * ny + iy + 1]);
+  return clamp_bounds(lin(y, yy[iy], v0, yy[iy + 1], v1));
+}
+
+// One Catmull-Rom segment through (x0,p0)..(x3,p3) evaluated between x1 and
+// x2: BicubicCINT (CalculateBicubicSpline.h:62-110, Horner branch).
+template <typename T>
+__device__ __forceinline__ T cubic_seg(T x, T x0, T p0, T x1, T p1, T x2, T p2, T x3, T p3) {
+  const T step = x2 - x1;
+  const T fx = (x - x1) / step;
+  T m1 = step * (p2 - p0) / (x2 - x0);
+  T m2 = step * (p3 - p1) / (x3 - x1);
+  if (fx < T(0)) m2 = m1;
+  if (fx > T(1)) m1 = m2;
+  return ((((-T(2) * p2 + T(2) * p1 + m2 + m1) * fx + T(3) * p2 - T(3) * p1 - m2 - T(2) * m1) * fx +
+           m1) * fx + p1);
+}
+
+// Value of knot (i, j) of the surface, linearly extended by one knot beyond
+// each edge as CalculateBicubicSpline.h:145-331 does.
+template <typename T>
+__device__ __forceinline__ T surf_knot(const T* __restrict__ z, int nx, int ny, int i, int j) {
+  // extend along y first, then along x (same expressions as the reference)
+  auto zy = [&](int ii, int jj) -> T {
+    if (jj < 0) return T(2) * z[ii * ny + 0] - z[ii * ny + 1];
+    if (jj > ny - 1) return T(2) * z[ii * ny + ny - 1] - z[ii * ny + ny - 2];
+    return z[ii * ny + jj];
+  };
+  if (i < 0) return T(2) * zy(0, j) - zy(1, j);
+  if (i > nx - 1) return T(2) * zy(nx - 1, j) - zy(nx - 2, j);
+  return zy(i, j);
+}
+
+template <typename T>
+__device__ __forceinline__ T axis_at(const T* __restrict__ a, int n, int i) {
+  if (i < 0) return T(2) * a[0] - a[1];
+  if (i > n - 1) return T(2) * a[n - 1] - a[n - 2];
+  return a[i];
+}
+
+// Bicubic surface: four Catmull-Rom rows along x, then one along y
+// (CalculateBicubicSpline.h:145-331).
+template <typename T>
+__device__ __forceinline__ T eval_bicubic(const T* __restrict__ d, T x, T y, bool trunc) {
+  const int nx = (int)d[0];
+  const int ny = (int)d[1];
+  const T* xx = d + 2;
+  const T* yy = xx + nx;
+  const T* z = yy + ny;
+  if (trunc) {
+    if (x < xx[0]) x = xx[0];
+    if (x > xx[nx - 1]) x = xx[nx - 1];
+    if (y < yy[0]) y = yy[0];
+    if (y > yy[ny - 1]) y = yy[ny - 1];
+  }
+  const int ix = surface_index(x, xx, nx - 1);
+  const int iy = surface_index(y, yy, ny - 1);
+  const T a0 = axis_at(xx, nx, ix - 1), a1 = xx[ix], a2 = xx[ix + 1], a3 = axis_at(xx, nx, ix + 2);
+  T v[4];
+  T u[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int j = iy - 1 + r;
+    u[r] = axis_at(yy, ny, j);
+    v[r] = cubic_seg(x, a0, surf_knot(z, nx, ny, ix - 1, j), a1, surf_knot(z, nx, ny, ix, j), a2,
+                     surf_knot(z, nx, ny, ix + 1, j), a3, surf_knot(z, nx, ny, ix + 2, j));
+  }
+  return clamp_bounds(cubic_seg(y, u[0], v[0], u[1], v[1], u[2], v[2], u[3], v[3]));
+}
+
+}  // namespace gw

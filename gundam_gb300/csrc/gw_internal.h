@@ -1,0 +1,77 @@
+// gw_internal.h -- what the host side of libgw hands to the kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gw_layout.h"
+
+namespace gw {
+
+// Device-side status bits, OR-ed by kernels into DevView::status.
+enum : uint32_t {
+  kStatusCopyTimeout = 1u,   // a bounded wait on a bulk copy gave up
+  kStatusBadTile = 2u        // a tile descriptor failed its in-kernel check
+};
+
+// Every device pointer and size a launch needs.  Plain data, passed by value.
+struct DevView {
+  int precision;        // 0 = FP64, 1 = FP32
+  int n_params;
+  int n_bins;
+  int n_events;
+  int n_tiles;
+  int kpad;             // parameter points per row of the [param][kpad] arrays
+  int llh_type;
+  int has_prior;
+  int has_cap;
+  int n_tables;
+  int n_table_fns;
+  int tile_payload_bytes;  // shared-memory bytes reserved per payload stage
+  double cap;
+
+  const TileDesc* tiles;
+  const uint64_t* hdr;
+  const unsigned char* payload;
+  const uint16_t* evinfo;
+  const void* w0;             // T[n_events], bin-sorted
+  const int32_t* bin_slot;    // [n_bins + 1]
+  const void* pclamp;         // T2[n_params] = (lower, upper)
+  const uint8_t* pflags;      // [n_params], bit 0 = truncate (no extrapolation)
+  const double* mirror_lo;    // [n_params]
+  const double* mirror_hi;    // [n_params]
+  const double* prior_mean;   // [n_params]
+  const double* prior_icov;   // [n_params * n_params]
+  const double* data;         // [n_bins]
+  const TableDesc* tables;
+  const TableFn* table_fns;
+  const double* table_nodes;
+  void* table_arena;          // T
+  const int32_t* sorted_to_result;  // [n_events]
+
+  void* x;                    // T[n_params * kpad], mirrored parameter values
+  double* penalty;            // [kpad]
+  double2* partials;          // [n_slots * kpad]  (scratch)
+  double* llh_blocks;         // [kpad * llh_nblk] (scratch)
+  unsigned int* llh_counter;  // [kpad]           (scratch)
+  int llh_nblk;
+  double* event_weights;      // [n_events] in result order, or nullptr
+  uint32_t* status;
+};
+
+// Launchers (gw_kernels.cu).  All are asynchronous on `stream`.
+cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s);
+cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s);
+cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
+cudaError_t launch_batched(const DevView& v, int K, int kc, int threads, int grid, cudaStream_t s);
+cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2, double* llh,
+                            double* llh_stat, cudaStream_t s);
+
+// Shared memory a kernel shape needs, and how many CTAs fit on one SM.
+size_t plain_smem_bytes(const DevView& v);
+size_t batched_smem_bytes(const DevView& v, int kc, int threads);
+int plain_blocks_per_sm(const DevView& v);
+int batched_blocks_per_sm(const DevView& v, int kc, int threads);
+
+constexpr int kPlainThreads = 256;
+
+}  // namespace gw

@@ -1,0 +1,673 @@
+// gw_kernels.cu -- the sm_103a kernels of the reweighting engine.
+//
+// One likelihood evaluation of K parameter points is four launches:
+//   k_params    mirror the parameters (DialInputBuffer.cpp:44-89) and compute
+//               the prior penalty (LikelihoodInterface.cpp:186-215);
+//   k_table_fn  (only with device table functions) refill per-point tables;
+//   k_plain / k_batched
+//               stream the bin-sorted tiles through shared memory with bulk
+//               (TMA) copies, evaluate every dial, form each event's weight as
+//               an ordered product (EventDialCache.cpp:156-171) and reduce the
+//               weights and squared weights per (tile, bin) in FP64;
+//   k_bins_llh  add the (tile, bin) partial sums of each bin in a fixed order
+//               (Histogram.cpp:107-135), evaluate the per-bin likelihood
+//               (PoissonLogLikelihood.h:19-53 / BarlowBeestonBanff2022.h:150-294)
+//               and reduce it, deterministically, to one value per point.
+// The reference needs ~1 + n_types + 2*(2 + log2 max bin occupancy) launches
+// for the same work (CacheWeights.cpp:153-183, CacheRecursiveSums.cpp:282-352).
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "gw_dials.cuh"
+#include "gw_internal.h"
+
+namespace gw {
+namespace {
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+// ---------------------------------------------------------------------------
+// Bulk-copy (TMA) and mbarrier helpers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the barrier phase; gives up (returns false) after limit_ns.
+__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per tile copy
+
+// Thread 0: start the bulk copy of a tile's payload into a stage buffer.
+__device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned char* buf, uint64_t* bar) {
+  const TileDesc td = v.tiles[tile];
+  const uint32_t bytes = (uint32_t)td.payload_16b * 16u;
+  mbar_expect_tx(bar, bytes);
+  if (bytes > 0) bulk_load(buf, v.payload + td.payload_off, bytes, bar);
+}
+
+// ---------------------------------------------------------------------------
+// One dial.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T eval_dial(const DevView& v, uint64_t h, const T* __restrict__ pl, int k) {
+  const int type = hdr_type(h);
+  const int n = hdr_n(h);
+  const T* d = pl + hdr_off(h);
+  const int p0 = hdr_p0(h);
+  T val, lo, hi;
+  if (type >= kTabulated) {
+    // Tabulated.h:27-28 and Kriged.cpp:14-21; clamp of the table's dials.
+    const TableDesc td = v.tables[p0];
+    lo = (T)td.lower;
+    hi = (T)td.upper;
+    const int64_t stride = td.per_k ? v.kpad : 1;
+    const T* tab = (const T*)v.table_arena + td.offset + (td.per_k ? k : 0);
+    if (type == kTabulated) {
+      const T f = d[0];
+      const int idx = (int)d[1];
+      val = f * tab[idx * stride] + (T(1) - f) * tab[(idx + 1) * stride];
+    } else {
+      val = T(0);
+      for (int j = 0; j < n; ++j) val += d[n + j] * tab[(int64_t)(int)d[j] * stride];
+    }
+  } else {
+    const T* xs = (const T*)v.x;
+    const T x = xs[(size_t)p0 * v.kpad + k];
+    const typename Vec2<T>::type c = ((const typename Vec2<T>::type*)v.pclamp)[p0];
+    lo = c.x;
+    hi = c.y;
+    const bool trunc = (v.pflags[p0] & 1) != 0;
+    switch (type) {
+      case kNorm: val = x; break;
+      case kMonotonic: val = eval_catmull<T, true>(d, n, x, trunc); break;
+      case kCompact: val = eval_catmull<T, false>(d, n, x, trunc); break;
+      case kUniform: val = eval_uniform<T>(d, n, x, trunc); break;
+      case kGeneral: val = eval_general<T>(d, n, x, trunc); break;
+      case kGraph: val = eval_graph<T>(d, n, x, trunc); break;
+      case kBilinear: {
+        const T y = xs[(size_t)hdr_p1(h) * v.kpad + k];
+        val = eval_bilinear<T>(d, x, y, trunc);
+        break;
+      }
+      case kBicubic: {
+        const T y = xs[(size_t)hdr_p1(h) * v.kpad + k];
+        val = eval_bicubic<T>(d, x, y, trunc);
+        break;
+      }
+      default: return T(1);
+    }
+  }
+  // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
+  if (val < lo) val = lo;
+  else if (val > hi) val = hi;
+  return val;
+}
+
+// ---------------------------------------------------------------------------
+// Parameter update: mirror into the dial inputs, prior penalty.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_params(const DevView v, const double* __restrict__ params) {
+  extern __shared__ double sp[];  // raw parameter vector of point k
+  const int k = blockIdx.x;
+  const int P = v.n_params;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) sp[p] = params[(size_t)k * P + p];
+  __syncthreads();
+  T* xs = (T*)v.x;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    double x = sp[p];
+    const double lo = v.mirror_lo[p], hi = v.mirror_hi[p];
+    if (lo > -DBL_MAX && hi < DBL_MAX) {
+      // DialInputBuffer.cpp:56-70
+      const double range = hi - lo;
+      double t = fabs(fmod(x - lo, 2 * range));
+      if (t > range) {
+        t -= 2 * range;
+        t = -t;
+      }
+      x = t + lo;
+    }
+    xs[(size_t)p * v.kpad + k] = (T)x;
+  }
+  if (!v.has_prior) return;
+  // delta^T C^-1 delta with u = C^-1 delta formed row by row.
+  double acc = 0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const double* row = v.prior_icov + (size_t)i * P;
+    double u = 0;
+    for (int j = 0; j < P; ++j) u += row[j] * (sp[j] - v.prior_mean[j]);
+    acc += (sp[i] - v.prior_mean[i]) * u;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double t = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) v.penalty[k] = t;
+  }
+}
+
+// Device table functions: one thread per (entry, point).
+template <typename T>
+__global__ void k_table_fn(const DevView v, int K) {
+  const TableFn fn = v.table_fns[blockIdx.y];
+  const TableDesc td = v.tables[fn.table];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= td.size) return;
+  const T* xs = (const T*)v.x;
+  const double E = v.table_nodes[fn.nodes + j];
+  T* arena = (T*)v.table_arena;
+  for (int k = 0; k < K; ++k) {
+    double q[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) q[i] = (double)xs[(size_t)fn.par[i] * v.kpad + k];
+    double val = 1.0;
+    if (fn.kind == 1) {
+      const double s = sin(q[1] * 1.267 / E + q[2]);
+      val = 1.0 - q[0] * s * s * (1.0 + q[3] * (log(E) - q[4])) * q[5];
+    }
+    arena[td.offset + (int64_t)j * v.kpad + k] = (T)val;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K = 1: type-ordered dial evaluation, one thread per dial.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int TB = v.tile_payload_bytes;
+  unsigned char* stage0 = smem;
+  unsigned char* stage1 = smem + TB;
+  T* dval = (T*)(smem + 2 * TB);                       // [1024]
+  double* wsh = (double*)(smem + 2 * TB + 1024 * sizeof(T));  // [kMaxTileEvents]
+  uint16_t* sev = (uint16_t*)(wsh + kMaxTileEvents);  // [kMaxTileEvents]
+  __shared__ uint64_t bar[2];
+  __shared__ int s_bstart[kMaxLocalBins], s_bend[kMaxLocalBins];
+
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int tile = blockIdx.x;
+  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
+  for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
+    const int st = it & 1;
+    const uint32_t parity = (uint32_t)((it >> 1) & 1);
+    const int next = tile + gridDim.x;
+    if (tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+
+    const TileDesc td = v.tiles[tile];
+    uint64_t h[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = tid + j * kPlainThreads;
+      h[j] = (i < td.ndials) ? v.hdr[td.dial0 + i] : 0ull;
+    }
+    T w0 = T(1);
+    uint16_t evi = 0;
+    if (tid < td.nevents) {
+      evi = v.evinfo[td.event0 + tid];
+      w0 = ((const T*)v.w0)[td.event0 + tid];
+      sev[tid] = evi;
+    }
+    if (tid < kMaxLocalBins) {
+      s_bstart[tid] = 0;
+      s_bend[tid] = 0;
+    }
+    const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(v.status, kStatusCopyTimeout);
+        if (next < v.n_tiles) mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      }
+      return;
+    }
+    const T* pl = (const T*)(st ? stage1 : stage0);
+
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = tid + j * kPlainThreads;
+      if (i < td.ndials) dval[hdr_slot(h[j])] = eval_dial<T>(v, h[j], pl, 0);
+    }
+    __syncthreads();
+
+    if (tid < td.nevents) {
+      const int s0 = ev_slot(evi);
+      const int s1 = (tid + 1 < td.nevents) ? ev_slot(sev[tid + 1]) : (int)td.ndials;
+      T w = T(1);
+      for (int s = s0; s < s1; ++s) w *= dval[s];
+      if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
+      w = w0 * w;
+      wsh[tid] = (double)w;
+      if (v.event_weights) v.event_weights[v.sorted_to_result[td.event0 + tid]] = (double)w;
+      const int lb = ev_lbin(evi);
+      if (tid == 0 || ev_lbin(sev[tid - 1]) != lb) s_bstart[lb] = tid;
+      if (tid + 1 == td.nevents || ev_lbin(sev[tid + 1]) != lb) s_bend[lb] = tid + 1;
+    }
+    __syncthreads();
+
+    // One warp per local bin: fixed-order FP64 reduction of w and w^2.
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < (int)td.nbins) {
+      const int b0 = s_bstart[warp], b1 = s_bend[warp];
+      if (b1 > b0) {
+        double s = 0.0, s2 = 0.0;
+        for (int e = b0 + lane; e < b1; e += 32) {
+          const double w = wsh[e];
+          s += w;
+          s2 += w * w;
+        }
+        for (int o = 16; o; o >>= 1) {
+          s += __shfl_xor_sync(0xffffffffu, s, o);
+          s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+          const int slot = (warp == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + warp];
+          v.partials[(size_t)slot * v.kpad] = make_double2(s, s2);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K > 1: events in order, lanes = parameter points.  KC points share one
+// warp pass (32/KC events per pass); the tile payload is read from HBM once
+// for all K points.
+// ---------------------------------------------------------------------------
+template <typename T, int KC, int NT>
+__global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
+  constexpr int NW = NT / 32;
+  constexpr int EPW = 32 / KC;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int TB = v.tile_payload_bytes;
+  unsigned char* stage0 = smem;
+  unsigned char* stage1 = smem + TB;
+  uint64_t* shdr = (uint64_t*)(smem + 2 * TB);                    // [1024]
+  double2* wpart = (double2*)(shdr + 1024);                       // [8][NW][32]
+  T* sw0 = (T*)(wpart + kMaxLocalBins * NW * 32);                 // [256]
+  uint16_t* sinv = (uint16_t*)(sw0 + kMaxTileEvents);             // [1024]
+  uint16_t* sev = sinv + 1024;                                    // [257]
+  __shared__ uint64_t bar[2];
+  __shared__ int s_present[kMaxLocalBins];
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int tile = blockIdx.x;
+  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
+  for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
+    const int st = it & 1;
+    const uint32_t parity = (uint32_t)((it >> 1) & 1);
+    const int next = tile + gridDim.x;
+    if (tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+
+    const TileDesc td = v.tiles[tile];
+    const int nd = td.ndials, ne = td.nevents;
+    for (int i = tid; i < nd; i += NT) {
+      const uint64_t h = v.hdr[td.dial0 + i];
+      shdr[i] = h;
+      sinv[hdr_slot(h)] = (uint16_t)i;
+    }
+    for (int e = tid; e < ne; e += NT) {
+      sev[e] = v.evinfo[td.event0 + e];
+      sw0[e] = ((const T*)v.w0)[td.event0 + e];
+    }
+    if (tid == 0) sev[ne] = make_evinfo(nd, 0);
+    if (tid < kMaxLocalBins) s_present[tid] = 0;
+    const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(v.status, kStatusCopyTimeout);
+        if (next < v.n_tiles) mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      }
+      return;
+    }
+    for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
+    const T* pl = (const T*)(st ? stage1 : stage0);
+
+    const int chunk = (ne + NW - 1) / NW;
+    const int e_lo = warp * chunk;
+    const int e_hi = min(ne, e_lo + chunk);
+    const int sub = lane / KC, kl = lane % KC;
+
+    for (int kc = 0; kc < K; kc += KC) {
+      const int k = kc + kl;
+#pragma unroll
+      for (int lb = 0; lb < kMaxLocalBins; ++lb) wpart[(lb * NW + warp) * 32 + lane] = make_double2(0.0, 0.0);
+      int cur = -1;
+      double s = 0.0, s2 = 0.0;
+      for (int base = e_lo; base < e_hi; base += EPW) {
+        const int e = base + sub;
+        if (e < e_hi) {
+          const uint16_t ei = sev[e];
+          const int s0 = ev_slot(ei), s1 = ev_slot(sev[e + 1]);
+          T w = T(1);
+          for (int sl = s0; sl < s1; ++sl) w *= eval_dial<T>(v, shdr[sinv[sl]], pl, k);
+          if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
+          w = sw0[e] * w;
+          const int lb = ev_lbin(ei);
+          if (lb != cur) {
+            if (cur >= 0) wpart[(cur * NW + warp) * 32 + lane] = make_double2(s, s2);
+            cur = lb;
+            s = 0.0;
+            s2 = 0.0;
+          }
+          const double wd = (double)w;
+          s += wd;
+          s2 += wd * wd;
+        }
+      }
+      if (cur >= 0) wpart[(cur * NW + warp) * 32 + lane] = make_double2(s, s2);
+      __syncthreads();
+      for (int t = tid; t < kMaxLocalBins * KC; t += NT) {
+        const int lb = t / KC, kk = t % KC;
+        const int kg = kc + kk;
+        if (kg < K && lb < (int)td.nbins && s_present[lb]) {
+          double a = 0.0, a2 = 0.0;
+          for (int w = 0; w < NW; ++w) {
+#pragma unroll
+            for (int sb = 0; sb < EPW; ++sb) {
+              const double2 p = wpart[(lb * NW + w) * 32 + sb * KC + kk];
+              a += p.x;
+              a2 += p.y;
+            }
+          }
+          const int slot = (lb == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + lb];
+          v.partials[(size_t)slot * v.kpad + kg] = make_double2(a, a2);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bin sums and likelihood.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double llh_poisson(double data, double pred) {
+  // PoissonLogLikelihood.h:19-53
+  if (pred <= 0.0) return HUGE_VAL;
+  if (data <= 0.0) return 2.0 * pred;
+  return 2.0 * (pred - data + data * log(data / pred));
+}
+
+__device__ __forceinline__ double llh_bb_oa2021(double data, double pred, double mcuncert) {
+  // BarlowBeestonBanff2022.h:150-294 with its defaults (expectedValueMinimum
+  // = -1, fractionalErrorLimit = 1e150, usePoissonLikelihood = false).
+  if (pred <= -1.0) {
+    if (pred <= 0.0 && data > 0.0) return HUGE_VAL;
+    return 0.0;
+  }
+  double newmc = pred;
+  double penalty = 0.0;
+  if (mcuncert > 0.0) {
+    const double fractional = fmin(sqrt(mcuncert) / pred, 1.0e150);
+    const double temp = pred * fractional * fractional - 1;
+    const double temp2 = temp * temp + 4 * data * fractional * fractional;
+    if (temp2 < 0) return HUGE_VAL;
+    const double beta = (-1 * temp + sqrt(temp2)) / 2.;
+    newmc = fmax(pred * beta, DBL_MIN);
+    penalty = (beta - 1) * (beta - 1) / (2 * fractional * fractional);
+  }
+  double stat;
+  if (data <= DBL_EPSILON) {
+    stat = newmc;
+  } else if (newmc > DBL_MIN) {
+    stat = newmc - data + data * (log(data) - log(newmc));
+  } else {
+    const double mc = DBL_MIN;
+    stat = mc - data + data * (log(data) - log(mc));
+  }
+  return 2.0 * stat + 2.0 * penalty;
+}
+
+__global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double* sums, double* sums2,
+                                                  double* llh, double* llh_stat) {
+  const int k = blockIdx.y;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  double term = 0.0;
+  if (b < v.n_bins) {
+    double s = 0.0, s2 = 0.0;
+    const int i0 = v.bin_slot[b], i1 = v.bin_slot[b + 1];
+    for (int i = i0; i < i1; ++i) {
+      const double2 p = v.partials[(size_t)i * v.kpad + k];
+      s += p.x;
+      s2 += p.y;
+    }
+    if (sums) sums[(size_t)k * v.n_bins + b] = s;
+    if (sums2) sums2[(size_t)k * v.n_bins + b] = s2;
+    if (v.llh_type == 1) {
+      term = llh_poisson(v.data[b], s);
+    } else if (v.llh_type == 2) {
+      const double err = sqrt(s2);  // BinContent::sqrtSumSqWeights, squared again by the LLH
+      term = llh_bb_oa2021(v.data[b], s, err * err);
+    }
+  }
+  if (v.llh_type == 0 || (llh == nullptr && llh_stat == nullptr)) return;
+  __shared__ double red[32];
+  __shared__ bool last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int o = 16; o; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+  if (lane == 0) red[warp] = term;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double t = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) {
+      v.llh_blocks[(size_t)k * v.llh_nblk + blockIdx.x] = t;
+      __threadfence();
+      const unsigned prev = atomicAdd(&v.llh_counter[k], 1u);
+      last = (prev == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  if (warp == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (int i = lane; i < (int)gridDim.x; i += 32) t += __ldcg(&v.llh_blocks[(size_t)k * v.llh_nblk + i]);
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) {
+      const double pen = v.has_prior ? v.penalty[k] : 0.0;
+      if (llh_stat) llh_stat[k] = t;
+      if (llh) llh[k] = t + pen;
+      v.llh_counter[k] = 0u;
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------
+size_t plain_smem_bytes(const DevView& v) {
+  const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  return 2 * (size_t)v.tile_payload_bytes + 1024 * tsz + kMaxTileEvents * sizeof(double) +
+         kMaxTileEvents * sizeof(uint16_t);
+}
+
+size_t batched_smem_bytes(const DevView& v, int kc, int threads) {
+  (void)kc;
+  const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  const int nw = threads / 32;
+  return 2 * (size_t)v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
+         (size_t)kMaxLocalBins * nw * 32 * sizeof(double2) + kMaxTileEvents * tsz +
+         1024 * sizeof(uint16_t) + (kMaxTileEvents + 1) * sizeof(uint16_t);
+}
+
+template <typename T>
+static const void* plain_fn() {
+  return (const void*)k_plain<T>;
+}
+
+template <typename T>
+static const void* batched_fn(int kc, int threads) {
+  if (threads == 128) {
+    if (kc == 8) return (const void*)k_batched<T, 8, 128>;
+    if (kc == 16) return (const void*)k_batched<T, 16, 128>;
+    return (const void*)k_batched<T, 32, 128>;
+  }
+  if (kc == 8) return (const void*)k_batched<T, 8, 256>;
+  if (kc == 16) return (const void*)k_batched<T, 16, 256>;
+  return (const void*)k_batched<T, 32, 256>;
+}
+
+static const void* pick_plain(const DevView& v) {
+  return v.precision ? plain_fn<float>() : plain_fn<double>();
+}
+
+static const void* pick_batched(const DevView& v, int kc, int threads) {
+  return v.precision ? batched_fn<float>(kc, threads) : batched_fn<double>(kc, threads);
+}
+
+int plain_blocks_per_sm(const DevView& v) {
+  const void* fn = pick_plain(v);
+  const size_t smem = plain_smem_bytes(v);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kPlainThreads, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+int batched_blocks_per_sm(const DevView& v, int kc, int threads) {
+  const void* fn = pick_batched(v, kc, threads);
+  const size_t smem = batched_smem_bytes(v, kc, threads);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s) {
+  const size_t smem = (size_t)v.n_params * sizeof(double);
+  const void* fn = v.precision ? (const void*)k_params<float> : (const void*)k_params<double>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (v.precision)
+    k_params<float><<<K, 256, smem, s>>>(v, params);
+  else
+    k_params<double><<<K, 256, smem, s>>>(v, params);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s) {
+  if (v.n_table_fns == 0) return cudaSuccess;
+  dim3 grid((max_size + 255) / 256, v.n_table_fns);
+  if (v.precision)
+    k_table_fn<float><<<grid, 256, 0, s>>>(v, K);
+  else
+    k_table_fn<double><<<grid, 256, 0, s>>>(v, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
+  const size_t smem = plain_smem_bytes(v);
+  if (v.precision)
+    k_plain<float><<<grid, kPlainThreads, smem, s>>>(v);
+  else
+    k_plain<double><<<grid, kPlainThreads, smem, s>>>(v);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static void launch_batched_t(const DevView& v, int K, int kc, int threads, int grid, size_t smem,
+                             cudaStream_t s) {
+  if (threads == 128) {
+    if (kc == 8) k_batched<T, 8, 128><<<grid, 128, smem, s>>>(v, K);
+    else if (kc == 16) k_batched<T, 16, 128><<<grid, 128, smem, s>>>(v, K);
+    else k_batched<T, 32, 128><<<grid, 128, smem, s>>>(v, K);
+  } else {
+    if (kc == 8) k_batched<T, 8, 256><<<grid, 256, smem, s>>>(v, K);
+    else if (kc == 16) k_batched<T, 16, 256><<<grid, 256, smem, s>>>(v, K);
+    else k_batched<T, 32, 256><<<grid, 256, smem, s>>>(v, K);
+  }
+}
+
+cudaError_t launch_batched(const DevView& v, int K, int kc, int threads, int grid, cudaStream_t s) {
+  const size_t smem = batched_smem_bytes(v, kc, threads);
+  if (v.precision)
+    launch_batched_t<float>(v, K, kc, threads, grid, smem, s);
+  else
+    launch_batched_t<double>(v, K, kc, threads, grid, smem, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2, double* llh,
+                            double* llh_stat, cudaStream_t s) {
+  dim3 grid(v.llh_nblk, K);
+  k_bins_llh<<<grid, 256, 0, s>>>(v, K, sums, sums2, llh, llh_stat);
+  return cudaGetLastError();
+}
+
+}  // namespace gw

@@ -1,0 +1,263 @@
+/*
+ * gw.h -- C ABI of the GB300 event-reweighting engine (libgw.so).
+ *
+ * This is the drop-in boundary for GUNDAM's Cache::Manager GPU path.  Every
+ * entry point is `extern "C"`, takes plain pointers and sizes, and returns an
+ * int status (GW_OK == 0).  No C++ exception crosses the boundary; the text of
+ * the last failure is returned by gw_last_error().
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the GUNDAM source tree).  The reference drives its cache through
+ * a per-type operator API filled by Cache::Manager::Update
+ * (src/CacheManager/src/CacheManager.cpp:477-740) and evaluated by
+ * Cache::Manager::Fill (src/CacheManager/src/CacheManager.cpp:750-810); the
+ * same calls exist here with the same argument meaning.
+ *
+ * Semantics follow the reference's CPU propagation, which is the oracle:
+ *   - norm dials are clamped like every other dial
+ *     (src/DialDictionary/DialEngine/src/DialCollection.cpp:453-454);
+ *   - the event-weight cap applies to the dial product before the base weight
+ *     (src/DialDictionary/DialEngine/src/EventDialCache.cpp:156-171);
+ *   - empty histogram bins sum to 0 (src/SamplesManager/src/Histogram.cpp:107-135);
+ *   - parameter mirroring uses the fmod form
+ *     (src/DialDictionary/DialEngine/src/DialInputBuffer.cpp:44-89).
+ *
+ * Threading: one host thread per engine at a time.  Calls on different engines
+ * are independent.
+ */
+#ifndef GW_H
+#define GW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  GW_OK = 0,
+  GW_ERR_ARG = 1,            /* bad argument (index out of range, bad size) */
+  GW_ERR_STATE = 2,          /* call not valid in the engine's current state */
+  GW_ERR_CUDA = 3,           /* CUDA runtime error */
+  GW_ERR_NOMEM = 4,          /* host or device allocation failed */
+  GW_ERR_LIMIT = 5,          /* a layout limit was exceeded (see gw_last_error) */
+  GW_ERR_DEVICE_TIMEOUT = 6, /* a bounded device-side wait gave up */
+  GW_ERR_NOT_FINITE = 7      /* a non-finite table entry or parameter */
+};
+
+/* ---- dial types (one per Cache::Weight::* calculator) ------------------ */
+enum {
+  GW_DIAL_NORM = 1,      /* Cache::Weight::Normalization  (WeightNormalization.cpp:96-118) */
+  GW_DIAL_MONOTONIC = 2, /* Cache::Weight::MonotonicSpline (WeightMonotonicSpline.cpp:286-321) */
+  GW_DIAL_UNIFORM = 3,   /* Cache::Weight::UniformSpline  (WeightUniformSpline.cpp:276-326) */
+  GW_DIAL_GENERAL = 4,   /* Cache::Weight::GeneralSpline  (WeightGeneralSpline.cpp:248-306) */
+  GW_DIAL_COMPACT = 5,   /* Cache::Weight::CompactSpline  (WeightCompactSpline.cpp:252-288) */
+  GW_DIAL_GRAPH = 6,     /* Cache::Weight::Graph          (WeightGraph.cpp:264-290) */
+  GW_DIAL_BILINEAR = 7,  /* Cache::Weight::Bilinear       (WeightBilinear.cpp:152-181) */
+  GW_DIAL_BICUBIC = 8,   /* Cache::Weight::Bicubic        (WeightBicubic.cpp:151-181) */
+  GW_DIAL_TABULATED = 9, /* Cache::Weight::Tabulated      (WeightTabulated.cpp:134-150) */
+  GW_DIAL_KRIGED = 10    /* Cache::Weight::Kriged         (WeightKriged.cpp:178-202) */
+};
+
+/* ---- precision of dial math and of the per-event weight product -------- */
+enum {
+  GW_FP64 = 0, /* everything in FP64, as the reference (WeightBase.h:19) */
+  GW_FP32 = 1  /* dials + weight product in FP32; bin sums, sum of w^2, LLH in FP64 */
+};
+
+/* ---- likelihood evaluated after the histogram step --------------------- */
+enum {
+  GW_LLH_NONE = 0,
+  GW_LLH_POISSON = 1,                /* PoissonLogLikelihood.h:19-53 */
+  GW_LLH_BARLOW_BEESTON_OA2021 = 2   /* BarlowBeestonBanff2022.h:150-294 ("BarlowLLH_BANFF_OA2021") */
+};
+
+/* ---- device table functions (tables recomputed on the GPU) ------------- */
+enum {
+  /* T_j = 1 - a*sin^2(b*1.267/E_j + c)*(1 + d*(ln E_j - e))*f, parameters
+   * (a,b,c,d,e,f) read from six fit parameters. */
+  GW_TABLE_FN_OSCILLATION = 1
+};
+
+typedef struct gw_engine gw_engine;
+
+/* Sizes fixed at construction.  Mirrors Cache::Manager::Build's counting pass
+ * (CacheManager.cpp:198-475): results = cached events, params = cached
+ * parameters, bins = histogram cells over all samples. */
+typedef struct gw_config {
+  int32_t n_results;  /* events in the cache */
+  int32_t n_params;   /* parameters in the cache (<= 65535) */
+  int32_t n_bins;     /* global histogram cells */
+  int32_t k_max;      /* largest number of parameter points per gw_eval (>= 1) */
+  int32_t precision;  /* GW_FP64 or GW_FP32 */
+  int32_t device;     /* CUDA device ordinal */
+  int32_t tile_bytes; /* payload bytes per tile; 0 = default */
+  int32_t flags;      /* reserved, must be 0 */
+} gw_config;
+
+/* ---- engine lifetime --------------------------------------------------- */
+
+/* Cache::Manager::HasGPU (CacheManager.h:78; CacheParameters.cpp:24-79).
+ * Writes 1 when a usable CUDA device exists, else 0. */
+int gw_has_gpu(int32_t* has_gpu);
+
+/* new Cache::Manager(...) (CacheManager.cpp:46-188). */
+int gw_create(const gw_config* config, gw_engine** engine);
+
+/* Cache::Manager destructor. */
+int gw_destroy(gw_engine* engine);
+
+/* Copies the text of the last error on this engine (or, with engine == NULL,
+ * the last gw_create failure of this thread) into buf. Replaces LogThrow. */
+int gw_last_error(const gw_engine* engine, char* buf, size_t len);
+
+/* ---- Cache::Parameters (CacheParameters.h:53-73) ----------------------- */
+int gw_set_lower_mirror(gw_engine* e, int32_t par, double value); /* SetLowerMirror, CacheParameters.cpp:162-166 */
+int gw_set_upper_mirror(gw_engine* e, int32_t par, double value); /* SetUpperMirror, CacheParameters.cpp:174-178 */
+int gw_set_lower_clamp(gw_engine* e, int32_t par, double value);  /* SetLowerClamp,  CacheParameters.cpp:186-190 */
+int gw_set_upper_clamp(gw_engine* e, int32_t par, double value);  /* SetUpperClamp,  CacheParameters.cpp:198-202 */
+/* allowDialExtrapolation of the parameter's dials (DialCollection.h:200;
+ * MonotonicSpline.cpp:78-81; Graph.cpp:48-51). Default: allowed. */
+int gw_set_extrapolation(gw_engine* e, int32_t par, int32_t allow);
+
+/* ---- Cache::Weights (CacheWeights.h:68-122) ---------------------------- */
+int gw_set_initial_value(gw_engine* e, int32_t result, double value); /* SetInitialValue, CacheWeights.h:121 */
+/* Batched form: values[i] for results [first, first+n). */
+int gw_set_initial_values(gw_engine* e, int32_t first, int32_t n, const double* values);
+
+/* ---- dial calculators (per-dial operator API) -------------------------- */
+/* Normalization::ReserveNorm (WeightNormalization.h:65). */
+int gw_reserve_norm(gw_engine* e, int32_t result, int32_t par);
+/* {Monotonic,Uniform,General,Compact}Spline::AddSpline (WeightMonotonicSpline.h:113,
+ * WeightUniformSpline.h:103, WeightGeneralSpline.h:104, WeightCompactSpline.h:113).
+ * data is the dial's getDialData() vector:
+ *   MONOTONIC, COMPACT: [low, step, y_0 .. y_{n-1}]
+ *   UNIFORM:            [low, step, (y, dy/dx) x n]
+ *   GENERAL:            [low, step, (y, dy/dx, x) x n] */
+int gw_add_spline(gw_engine* e, int32_t type, int32_t result, int32_t par,
+                  const double* data, int32_t n_data);
+/* Graph::AddGraph (WeightGraph.h:89); data = [(y, x) x n]. */
+int gw_add_graph(gw_engine* e, int32_t result, int32_t par, const double* data, int32_t n_data);
+/* Bilinear::AddData / Bicubic::AddData (WeightBilinear.h:92, WeightBicubic.h:95);
+ * data = [nx, ny, x[nx], y[ny], z[nx*ny]] with z row-major over x. */
+int gw_add_surface(gw_engine* e, int32_t type, int32_t result, int32_t par1, int32_t par2,
+                   const double* data, int32_t n_data);
+/* Tabulated::AddData (WeightTabulated.h:57): v = f*T[index] + (1-f)*T[index+1]. */
+int gw_add_tabulated(gw_engine* e, int32_t result, int32_t table, int32_t index, double fraction);
+/* Kriged::AddData (WeightKriged.h:57): v = sum_j w_j * T[index_j]. */
+int gw_add_kriged(gw_engine* e, int32_t result, int32_t table, int32_t n,
+                  const int32_t* index, const float* weight);
+
+/* Batched form of all of the above (no reference counterpart; one call per
+ * block of dials).  Dial i has type[i], result[i], par0[i], par1[i] (-1 when
+ * unused) and data[data_start[i] .. data_start[i+1]) in the formats above;
+ * TABULATED data = [table, index, fraction], KRIGED data =
+ * [table, m, index_0..index_{m-1}, weight_0..weight_{m-1}]. */
+int gw_add_dials(gw_engine* e, int64_t n, const uint8_t* type, const int32_t* result,
+                 const int32_t* par0, const int32_t* par1, const int64_t* data_start,
+                 const double* data);
+
+/* ---- tables for TABULATED / KRIGED dials ------------------------------- */
+/* Registers a table of `size` entries (the std::vector<double>* a dial
+ * borrows in WeightTabulated.h:57 / WeightKriged.h:57). */
+int gw_create_table(gw_engine* e, int32_t size, int32_t* table);
+/* Host refresh of a table (WeightTabulated.cpp:161-171, WeightKriged.cpp:213-223).
+ * Takes effect at the next gw_eval. */
+int gw_set_table(gw_engine* e, int32_t table, const double* values, int32_t size);
+/* Response clamp of the table's dials (DialResponseSupervisor.cpp:10-18). */
+int gw_set_table_clamp(gw_engine* e, int32_t table, double lower, double upper);
+/* Recompute the table on the device from fit parameters at every point
+ * (replaces the host updateTable plugin, KrigedDialFactory.cpp:135-145).
+ * params[6] are fit-parameter indices, nodes[size] the energies E_j. */
+int gw_set_table_function(gw_engine* e, int32_t table, int32_t fn, const int32_t* params,
+                          int32_t n_params, const double* nodes, int32_t size);
+
+/* ---- Cache::HistogramSum (CacheRecursiveSums.h:84-152) ------------------ */
+int gw_set_event_index(gw_engine* e, int32_t result, int32_t bin);   /* SetEventIndex, CacheRecursiveSums.h:107 */
+int gw_set_event_indices(gw_engine* e, int32_t first, int32_t n, const int32_t* bins);
+int gw_set_maximum_event_weight(gw_engine* e, double maximum);        /* SetMaximumEventWeight, :111 */
+
+/* ---- likelihood (JointProbabilityBase.h:37-54; LikelihoodInterface.cpp:165-215) */
+int gw_set_data(gw_engine* e, const double* data, int32_t n_bins);
+int gw_set_likelihood(gw_engine* e, int32_t llh_type);
+/* Gaussian prior penalty (x-mean)^T inv_cov (x-mean) (LikelihoodInterface.cpp:186-215).
+ * inv_cov is n_params*n_params row-major; NULL clears the prior. */
+int gw_set_prior(gw_engine* e, const double* mean, const double* inv_cov);
+
+/* Packs, sorts, validates and uploads everything (RecursiveSums::Initialize,
+ * CacheRecursiveSums.cpp:92-153, plus the hemi uploads).  After this the
+ * builder calls above return GW_ERR_STATE. */
+int gw_initialize(gw_engine* e);
+
+/* ---- evaluation -------------------------------------------------------- */
+/* Cache::Manager::Fill + CopyHistogramContents + the per-bin likelihood
+ * (CacheManager.cpp:750-866; LikelihoodInterface.cpp:165-178), for K
+ * parameter points at once.  Host buffers:
+ *   params   [K * n_params]  parameter values (row k = point k)
+ *   sums     [K * n_bins]    sum of weights per bin        (may be NULL)
+ *   sums2    [K * n_bins]    sum of squared weights per bin (may be NULL)
+ *   llh      [K]             stat + penalty                 (may be NULL)
+ *   llh_stat [K]             stat part only                 (may be NULL)
+ * Blocks until the results are on the host. */
+int gw_eval(gw_engine* e, const double* params, int32_t K, double* sums, double* sums2,
+            double* llh, double* llh_stat);
+
+/* Same as gw_eval with DEVICE pointers, asynchronous on `stream`
+ * (a cudaStream_t; NULL = the engine's own stream).  Any output may be NULL. */
+int gw_eval_device(gw_engine* e, const double* d_params, int32_t K, double* d_sums,
+                   double* d_sums2, double* d_llh, double* d_llh_stat, void* stream);
+
+/* Waits for the engine's outstanding work and reports device-side errors
+ * (GW_ERR_DEVICE_TIMEOUT when a bounded wait gave up). */
+int gw_sync(gw_engine* e);
+
+/* Capture the K-point launch chain in a CUDA graph (on != 0) or go back to
+ * plain launches. */
+int gw_use_graph(gw_engine* e, int32_t on);
+
+/* Times the batched kernel shapes for K points and keeps the fastest
+ * (points per warp pass x threads per block). */
+int gw_autotune(gw_engine* e, int32_t K);
+
+/* Copies the chosen batched shape out (after gw_autotune). */
+int gw_get_shape(const gw_engine* e, int32_t* points_per_pass, int32_t* threads);
+
+/* Cache::Manager::SetIsEventWeightCopyEnabled (CacheManager.h:119). */
+int gw_set_event_weight_copy(gw_engine* e, int32_t enable);
+
+/* Cache::Manager::CopyEventWeights (CacheManager.cpp:812-843): the per-event
+ * weights of point 0 of the last gw_eval, in result order (n_results values).
+ * Requires gw_set_event_weight_copy(e, 1) before the evaluation. */
+int gw_get_event_weights(gw_engine* e, double* weights);
+
+/* Cache::Manager::GetResidentMemory (CacheManager.h:192): device bytes held. */
+int gw_resident_memory(const gw_engine* e, int64_t* bytes);
+
+/* Measurement hooks (no reference counterpart; the reference keeps averaged
+ * host timers, CacheManager.h:131-135).  With profiling on, every evaluation
+ * records CUDA events on its launch stream around the weights kernel. */
+int gw_set_profiling(gw_engine* e, int32_t on);
+/* Sum of the weights-kernel durations (ms) and counts since the last read;
+ * kernel_launches counts every engine kernel launched.  Resets the sums. */
+int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weights_launches, int64_t* kernel_launches);
+
+/* Layout facts for measurement: tiles, dials, payload bytes, algorithmic
+ * bytes read per evaluation pass. */
+typedef struct gw_layout_info {
+  int64_t n_tiles;
+  int64_t n_dials;
+  int64_t payload_bytes;
+  int64_t header_bytes;
+  int64_t event_bytes;
+  int64_t partial_slots;
+  int64_t dials_by_type[11];
+} gw_layout_info;
+int gw_get_layout(const gw_engine* e, gw_layout_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GW_H */

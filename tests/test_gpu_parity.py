@@ -1,0 +1,258 @@
+"""CUDA engine against the FP64 CPU oracle on the same seeded inputs.
+
+Tolerances (FP64 mode, as the acceptance bar states): per-bin relative error
+<= 1e-12 on the sum of weights and the sum of squared weights, likelihood
+absolute error <= 1e-6.  FP32 mode (dial math and weight product in FP32,
+bins / sum of w^2 / likelihood in FP64): per-bin relative error <= 2e-5 and
+likelihood absolute error <= 5e-2 (stated in FP32_* below).
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gundam_gb300 import Engine, Workload
+from gundam_gb300 import _native as N
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+FP64_BIN_REL = 1e-12
+FP64_LLH_ABS = 1e-6
+FP32_BIN_REL = 2e-5
+FP32_LLH_ABS = 5e-2
+
+
+def _bin_rel(got, ref):
+    got, ref = np.asarray(got), np.asarray(ref)
+    den = np.where(ref != 0, np.abs(ref), 1.0)
+    return float(np.max(np.abs(got - ref) / den))
+
+
+def _check(eng_out, orc, bin_rel, llh_abs, label=""):
+    sums, sums2, llh, stat = eng_out
+    assert _bin_rel(sums, orc["sums"]) <= bin_rel, label
+    assert _bin_rel(sums2, orc["sums2"]) <= bin_rel, label
+    fin = np.isfinite(orc["llh"])
+    assert np.array_equal(np.isfinite(llh), fin), label
+    assert np.max(np.abs(llh[fin] - orc["llh"][fin]), initial=0.0) <= llh_abs, label
+    assert np.max(np.abs(stat[fin] - orc["llh_stat"][fin]), initial=0.0) <= llh_abs, label
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return Workload("c1", seed=11)
+
+
+@pytest.fixture(scope="module")
+def c1_oracle(c1):
+    return Oracle(c1, llh_type=N.GW_LLH_POISSON)
+
+
+@pytest.fixture(scope="module")
+def mixed():
+    return Workload("mixed", seed=5)
+
+
+@pytest.fixture(scope="module")
+def mixed_oracle(mixed):
+    return Oracle(mixed, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+
+
+def test_c1_fp64_plain(c1, c1_oracle):
+    eng = Engine.from_workload(c1, precision="fp64", k_max=1, llh_type=N.GW_LLH_POISSON)
+    pts = np.vstack([c1.nominal(), c1.draw_points(24, 5)])
+    for i, p in enumerate(pts):
+        _check(eng.eval(p[None]), c1_oracle.eval(p[None]), FP64_BIN_REL, FP64_LLH_ABS, f"point {i}")
+    eng.close()
+
+
+def test_c1_fp32_plain(c1, c1_oracle):
+    eng = Engine.from_workload(c1, precision="fp32", k_max=1, llh_type=N.GW_LLH_POISSON)
+    pts = np.vstack([c1.nominal(), c1.draw_points(12, 6)])
+    for i, p in enumerate(pts):
+        _check(eng.eval(p[None]), c1_oracle.eval(p[None]), FP32_BIN_REL, FP32_LLH_ABS, f"point {i}")
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("K", [2, 16, 64, 200])
+def test_c1_batched(c1, c1_oracle, precision, K):
+    eng = Engine.from_workload(c1, precision=precision, k_max=256, llh_type=N.GW_LLH_POISSON)
+    pts = c1.draw_points(K, 100 + K)
+    ref = c1_oracle.eval(pts)
+    rel, ab = (FP64_BIN_REL, FP64_LLH_ABS) if precision == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
+    _check(eng.eval(pts), ref, rel, ab, f"K={K}")
+    eng.close()
+
+
+def test_batched_point_equals_plain_point(c1):
+    """Point k of a batch gives the same bins as evaluating it alone (FP64)."""
+    eng = Engine.from_workload(c1, precision="fp64", k_max=64)
+    pts = c1.draw_points(64, 77)
+    sb, s2b, lb, _ = eng.eval(pts)
+    for k in (0, 17, 63):
+        s, s2, l, _ = eng.eval(pts[k:k + 1])
+        assert _bin_rel(sb[k], s[0]) <= FP64_BIN_REL
+        assert abs(lb[k] - l[0]) <= FP64_LLH_ABS
+    eng.close()
+
+
+def test_mixed_all_dial_types_fp64(mixed, mixed_oracle):
+    """Every dial type, mirrored and truncated parameters, response clamps, the
+    weight cap, host tables, base weights != 1, events without dials and empty bins."""
+    eng = Engine.from_workload(mixed, precision="fp64", k_max=8, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    eng.set_event_weight_copy(True)
+    pts = np.vstack([mixed.nominal(), mixed.draw_points(15, 9, inflate=1.6)])
+    for i, p in enumerate(pts):
+        ref = mixed_oracle.eval(p[None], weights=True)
+        out = eng.eval(p[None])
+        _check(out, ref, FP64_BIN_REL, FP64_LLH_ABS, f"point {i}")
+        w = eng.event_weights()
+        assert _bin_rel(w, ref["weights"]) <= 1e-13
+        counts = np.bincount(mixed.event_bin, minlength=mixed.n_bins)
+        assert np.any(counts == 0) and np.all(out[0][0][counts == 0] == 0.0)
+    _check(eng.eval(pts[:8]), mixed_oracle.eval(pts[:8]), FP64_BIN_REL, FP64_LLH_ABS, "batched")
+    eng.close()
+
+
+def test_mixed_fp32(mixed, mixed_oracle):
+    eng = Engine.from_workload(mixed, precision="fp32", k_max=8, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    pts = mixed.draw_points(8, 19, inflate=1.4)
+    _check(eng.eval(pts), mixed_oracle.eval(pts), FP32_BIN_REL, FP32_LLH_ABS)
+    eng.close()
+
+
+def test_per_dial_api_equals_batched_api(mixed):
+    a = Engine.from_workload(mixed, precision="fp64", k_max=4)
+    b = Engine.from_workload(mixed, precision="fp64", k_max=4, per_dial=True)
+    pts = mixed.draw_points(4, 3)
+    ra, rb = a.eval(pts), b.eval(pts)
+    for x, y in zip(ra, rb):
+        np.testing.assert_array_equal(x, y)
+    a.close()
+    b.close()
+
+
+def test_graph_capture_gives_identical_results(c1):
+    eng = Engine.from_workload(c1, precision="fp32", k_max=64)
+    pts = c1.draw_points(64, 8)
+    plain = [eng.eval(pts), eng.eval(pts[:1])]
+    eng.use_graph(True)
+    graph = [eng.eval(pts), eng.eval(pts[:1]), eng.eval(pts)]
+    for x, y in zip(plain[0], graph[0]):
+        np.testing.assert_array_equal(x, y)
+    for x, y in zip(plain[1], graph[1]):
+        np.testing.assert_array_equal(x, y)
+    for x, y in zip(graph[0], graph[2]):
+        np.testing.assert_array_equal(x, y)
+    eng.close()
+
+
+def test_results_are_deterministic(c1):
+    eng = Engine.from_workload(c1, precision="fp64", k_max=32)
+    pts = c1.draw_points(32, 4)
+    r1, r2 = eng.eval(pts), eng.eval(pts)
+    for x, y in zip(r1, r2):
+        np.testing.assert_array_equal(x, y)
+    eng.close()
+
+
+def test_autotune_picks_a_valid_shape(c1, c1_oracle):
+    eng = Engine.from_workload(c1, precision="fp32", k_max=64)
+    eng.autotune(64)
+    kc, th = eng.shape()
+    assert kc in (8, 16, 32) and th in (128, 256)
+    pts = c1.draw_points(64, 12)
+    _check(eng.eval(pts), c1_oracle.eval(pts), FP32_BIN_REL, FP32_LLH_ABS)
+    eng.close()
+
+
+def test_event_weights_c1(c1, c1_oracle):
+    eng = Engine.from_workload(c1, precision="fp64", k_max=1)
+    eng.set_event_weight_copy(True)
+    p = c1.draw_points(1, 55)
+    eng.eval(p)
+    w = eng.event_weights()
+    ref = c1_oracle.eval(p, weights=True)["weights"]
+    assert _bin_rel(w, ref) <= 1e-13
+    eng.close()
+
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "dials.json").read_text())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_reference_golden_dials_through_engine(precision):
+    """One event per golden case, one dial per event, on its own parameter(s);
+    the event weight is the dial response computed by the reference's own
+    Calculate*.h."""
+    data = GOLDEN["data"]
+    cases = [c for c in GOLDEN["cases"] if abs(c[4]) < 1e19]
+    n = len(cases)
+    chunk = 2000
+    for s in range(0, n, chunk):
+        part = cases[s:s + chunk]
+        m = len(part)
+        P = 2 * m
+        eng = Engine(m, P, 1, k_max=1, precision=precision)
+        params = np.zeros(P)
+        for p in range(P):
+            eng.set_lower_clamp(p, -np.finfo(np.float64).max)
+        for i, (t, di, x, y, v) in enumerate(part):
+            d = data[di]
+            if t in (7, 8):
+                eng.add_surface(t, i, 2 * i, 2 * i + 1, d)
+            elif t == 6:
+                eng.add_graph(i, 2 * i, d)
+            else:
+                eng.add_spline(t, i, 2 * i, d)
+            params[2 * i] = x
+            params[2 * i + 1] = y
+        eng.set_event_indices(np.zeros(m, dtype=np.int32))
+        eng.initialize()
+        eng.set_event_weight_copy(True)
+        eng.eval(params[None])
+        w = eng.event_weights()
+        ref = np.array([c[4] for c in part])
+        if precision == "fp64":
+            tol = 1e-13 * np.maximum(1.0, np.abs(ref))
+        else:
+            tol = 1e-4 * np.maximum(1.0, np.abs(ref))
+        bad = np.nonzero(np.abs(w - ref) > tol)[0]
+        assert bad.size == 0, [(part[i][0], part[i][2], part[i][3], ref[i], w[i]) for i in bad[:5]]
+        eng.close()
+
+
+def test_c2_subset_fp64_and_fp32():
+    wl = Workload("c2", n_events=300000, seed=21)
+    orc = Oracle(wl, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    pts = np.vstack([wl.nominal(), wl.draw_points(5, 2)])
+    ref = orc.eval(pts)
+    e64 = Engine.from_workload(wl, precision="fp64", k_max=8)
+    _check(e64.eval(pts), ref, FP64_BIN_REL, FP64_LLH_ABS, "c2 fp64 batched")
+    for i in range(2):
+        _check(e64.eval(pts[i:i + 1]), orc.eval(pts[i:i + 1]), FP64_BIN_REL, FP64_LLH_ABS, "c2 fp64 plain")
+    e64.close()
+    e32 = Engine.from_workload(wl, precision="fp32", k_max=8)
+    _check(e32.eval(pts), ref, FP32_BIN_REL, FP32_LLH_ABS, "c2 fp32")
+    e32.close()
+
+
+def test_device_pointer_entry_point(c1, c1_oracle):
+    torch = pytest.importorskip("torch")
+    eng = Engine.from_workload(c1, precision="fp64", k_max=16)
+    pts = c1.draw_points(16, 31)
+    d_p = torch.from_numpy(pts).cuda()
+    d_s = torch.empty((16, c1.n_bins), dtype=torch.float64, device="cuda")
+    d_s2 = torch.empty_like(d_s)
+    d_l = torch.empty(16, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    eng.eval_device(d_p.data_ptr(), 16, d_s.data_ptr(), d_s2.data_ptr(), d_l.data_ptr(), 0, stream)
+    torch.cuda.synchronize()
+    eng.sync()
+    ref = c1_oracle.eval(pts)
+    assert _bin_rel(d_s.cpu().numpy(), ref["sums"]) <= FP64_BIN_REL
+    assert np.max(np.abs(d_l.cpu().numpy() - ref["llh"])) <= FP64_LLH_ABS
+    eng.close()
