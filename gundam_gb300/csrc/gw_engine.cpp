@@ -966,6 +966,7 @@ int build_and_upload(gw_engine* e) {
   L.partial_slots = e->n_slots;
   for (const DialRec& r : e->dials) L.dials_by_type[r.type]++;
 
+  GW_CUDA(e, prepare_params(v));
   // grids
   const int bps = plain_blocks_per_sm(v);
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
@@ -1006,6 +1007,7 @@ static int refresh_tables(gw_engine* e) {
   const size_t tsz = e->cfg.precision == GW_FP32 ? 4 : 8;
   // table offsets are recomputed in creation order (same as the upload)
   int64_t off = 0;
+  bool copied = false;
   for (HostTable& h : e->tables) {
     if (!h.has_fn && h.dirty) {
       unsigned char* dst = (unsigned char*)e->view.table_arena + off * tsz;
@@ -1018,9 +1020,12 @@ static int refresh_tables(gw_engine* e) {
         GW_CUDA(e, cudaStreamSynchronize(e->stream));
       }
       h.dirty = false;
+      copied = true;
     }
     off += h.has_fn ? (int64_t)h.size * e->kpad : h.size;
   }
+  // a launch on another stream must see the new tables
+  if (copied) GW_CUDA(e, cudaStreamSynchronize(e->stream));
   return GW_OK;
 }
 

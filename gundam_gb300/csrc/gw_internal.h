@@ -59,6 +59,7 @@ struct DevView {
 };
 
 // Launchers (gw_kernels.cu).  All are asynchronous on `stream`.
+cudaError_t prepare_params(const DevView& v);  // once, before any launch or capture
 cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s);
 cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s);
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);

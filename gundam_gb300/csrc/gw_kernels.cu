@@ -609,11 +609,14 @@ int batched_blocks_per_sm(const DevView& v, int kc, int threads) {
   return n;
 }
 
-cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s) {
+cudaError_t prepare_params(const DevView& v) {
   const size_t smem = (size_t)v.n_params * sizeof(double);
   const void* fn = v.precision ? (const void*)k_params<float> : (const void*)k_params<double>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s) {
+  const size_t smem = (size_t)v.n_params * sizeof(double);
   if (v.precision)
     k_params<float><<<K, 256, smem, s>>>(v, params);
   else
