@@ -182,7 +182,9 @@ def run_reference(args, world, rank, dist):
 
 
 def time_device(eng, torch, d, K, steps, warmup, dist):
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the legacy default stream has handle 0, which the
+    # C ABI reads as "the engine's own stream"
+    stream = d.setdefault("stream", torch.cuda.Stream())
     sp = stream.cuda_stream
     for _ in range(warmup):
         eng.eval_device(d["p"].data_ptr(), K, d["s"].data_ptr(), d["s2"].data_ptr(), d["l"].data_ptr(), 0, sp)
