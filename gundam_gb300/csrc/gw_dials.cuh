@@ -12,6 +12,11 @@
 
 namespace gw {
 
+// Division: IEEE in FP64 mode (parity with the reference), the fast
+// reciprocal-multiply form in FP32 mode (within the FP32 tolerance).
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+
 template <typename T>
 __device__ __forceinline__ T clamp_bounds(T v) {
   const T lo = T(-1e20), hi = T(1e20);
@@ -118,7 +123,7 @@ __device__ __forceinline__ T eval_general(const T* __restrict__ d, int n, T x, b
   const T x1 = d[3 * ix + 2];
   const T x2 = d[3 * (ix + 1) + 2];
   const T step = x2 - x1;
-  const T fx = (x - x1) / step;
+  const T fx = fdiv(x - x1, step);
   const T p1 = d[3 * ix];
   const T m1 = d[3 * ix + 1] * step;
   const T p2 = d[3 * (ix + 1)];
@@ -145,9 +150,35 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
   const T p2 = d[2 * (ix + 1)];
   const T x2 = d[2 * (ix + 1) + 1];
   const T step = x2 - x1;
-  const T fx = (x - x1) / step;
+  const T fx = fdiv(x - x1, step);
   const T m = p2 - p1;
   return clamp_bounds(p1 + fx * m);
+}
+
+// FP32 layout of the Catmull-Rom and uniform splines.  The host stores each
+// knot's value and its slope in index units (for Catmull-Rom splines the
+// slope after the Fritsch-Carlson limiter, for uniform splines dydx*step) and
+// 1/step instead of step: d = [low, 1/step, (y, s) x n].  Inside the knot
+// range this is exactly the Hermite cubic the reference evaluates; beyond the
+// ends the reference's clamped neighbour indices make the outer slope equal
+// the end difference (CalculateMonotonicSpline.h:66-103), restored here.
+template <bool catmull>
+__device__ __forceinline__ float eval_prepared(const float* __restrict__ d, int n, float x, bool trunc) {
+  float xx = (x - d[0]) * d[1];
+  if (trunc) xx = fminf(fmaxf(xx, 0.f), (float)(n - 1));
+  const int ix = catmull ? ((xx < 0.f) ? (int)(xx - 1.f) : (int)xx) : (int)xx;
+  const int i = min(max(ix, 0), n - 2);
+  const float fx = xx - (float)i;
+  const float* k = d + 2 + 2 * i;
+  const float p1 = k[0];
+  float m1 = k[1];
+  const float p2 = k[2];
+  float m2 = k[3];
+  if (catmull) {
+    if (ix < 0) m2 = p2 - p1;
+    if (ix > n - 2) m1 = p2 - p1;
+  }
+  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
 }
 
 // Index of the facet for a value: BilinearIndex / BicubicIndex
@@ -164,7 +195,7 @@ __device__ __forceinline__ int surface_index(T v, const T* __restrict__ a, int n
 
 template <typename T>
 __device__ __forceinline__ T lin(T x, T x0, T p0, T x1, T p1) {
-  return p0 + (p1 - p0) * (x - x0) / (x1 - x0);
+  return p0 + fdiv((p1 - p0) * (x - x0), x1 - x0);
 }
 
 // Bilinear surface: CalculateBilinearInterpolation.h:103-152.
@@ -194,9 +225,9 @@ __device__ __forceinline__ T eval_bilinear(const T* __restrict__ d, T x, T y, bo
 template <typename T>
 __device__ __forceinline__ T cubic_seg(T x, T x0, T p0, T x1, T p1, T x2, T p2, T x3, T p3) {
   const T step = x2 - x1;
-  const T fx = (x - x1) / step;
-  T m1 = step * (p2 - p0) / (x2 - x0);
-  T m2 = step * (p3 - p1) / (x3 - x1);
+  const T fx = fdiv(x - x1, step);
+  T m1 = fdiv(step * (p2 - p0), x2 - x0);
+  T m2 = fdiv(step * (p3 - p1), x3 - x1);
   if (fx < T(0)) m2 = m1;
   if (fx > T(1)) m1 = m2;
   return ((((-T(2) * p2 + T(2) * p1 + m2 + m1) * fx + T(3) * p2 - T(3) * p1 - m2 - T(2) * m1) * fx +

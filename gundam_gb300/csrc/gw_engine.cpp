@@ -93,7 +93,8 @@ struct gw_engine {
   int kpad = 32;
   int n_slots = 0;
   int plain_grid = 1;
-  int batched_kc = 32, batched_threads = 256, batched_grid = 1;
+  BatchedShape shape{32, 2, 256, 1};
+  int batched_grid = 1;
   bool tuned = false;
   int max_fn_table = 0;
   std::vector<void*> dev_allocs;  // owned device allocations
@@ -590,6 +591,51 @@ void write_payload(const DialRec& r, const double* d, T* out) {
   }
 }
 
+// FP32 layout of Catmull-Rom (monotonic, compact) and uniform splines:
+// [low, 1/step, (y, s) x n] with s the knot slope in index units.  The
+// Catmull-Rom slope of knot k is the one CalculateMonotonicSpline.h:66-127
+// forms from its neighbours (with the Fritsch-Carlson limiter for monotonic
+// splines); the end knots get the end difference.  Computed here in FP64.
+void write_prepared(const DialRec& r, const double* d, int n, float* out) {
+  const double low = d[0], step = d[1];
+  out[0] = (float)low;
+  out[1] = (float)(1.0 / step);
+  if (r.type == kUniform) {
+    for (int k = 0; k < n; ++k) {
+      out[2 + 2 * k] = (float)d[2 + 2 * k];
+      out[3 + 2 * k] = (float)(d[3 + 2 * k] * step);
+    }
+    return;
+  }
+  const double* y = d + 2;
+  const bool limit = r.type == kMonotonic;
+  for (int k = 0; k < n; ++k) {
+    double s;
+    if (k == 0) {
+      s = y[1] - y[0];
+    } else if (k == n - 1) {
+      s = y[n - 1] - y[n - 2];
+    } else {
+      const double dl = y[k] - y[k - 1], dr = y[k + 1] - y[k];
+      s = 0.5 * (dl + dr);
+      if (limit) {
+        if (dr * dl <= 0.0) s = 0.0;
+        const double delta = 3.0 * std::min(std::fabs(dl), std::fabs(dr));
+        if (s > delta) s = delta;
+        if (s < -delta) s = -delta;
+      }
+    }
+    out[2 + 2 * k] = (float)y[k];
+    out[3 + 2 * k] = (float)s;
+  }
+}
+
+// Stored elements of a dial in the engine precision.
+int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool fp32) {
+  if (fp32 && (r.type == kMonotonic || r.type == kCompact)) return 2 + 2 * n;
+  return raw;
+}
+
 struct TilePlan {
   int64_t ev_begin, ev_end;  // into the sorted event list
   int32_t ndials;
@@ -636,7 +682,7 @@ int build_and_upload(gw_engine* e) {
             int64_t exp = -1;
             bad.compare_exchange_strong(exp, i);
           }
-          pel[(size_t)i] = (int32_t)el;
+          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, tsz == 4);
           pn[(size_t)i] = n;
         }
       });
@@ -771,7 +817,10 @@ int build_and_upload(gw_engine* e) {
             const int p0 = r.type >= kTabulated ? (int)e->dial_data[(size_t)r.data_off] : r.p0;
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
             hdr[(size_t)(tp.dial0 + j)] = make_header(r.type, pn[(size_t)di], slot, off, p0, p1);
-            write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
+            if (tsz == 4 && (r.type == kMonotonic || r.type == kCompact || r.type == kUniform))
+              write_prepared(r, e->dial_data.data() + r.data_off, pn[(size_t)di], (float*)(pl + off));
+            else
+              write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
             off += pel[(size_t)di];
           }
           TileDesc& d = tdesc[(size_t)ti];
@@ -802,7 +851,7 @@ int build_and_upload(gw_engine* e) {
   GW_CUDA(e, cudaSetDevice(e->device));
   GW_CUDA(e, cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device));
   GW_CUDA(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
-  e->kpad = ((e->cfg.k_max + 31) / 32) * 32;
+  e->kpad = ((e->cfg.k_max + 63) / 64) * 64;  // a batched pass covers up to 64 points
   const int P = e->cfg.n_params;
   const int kpad = e->kpad;
 
@@ -972,9 +1021,11 @@ int build_and_upload(gw_engine* e) {
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
   e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bps * e->num_sms));
   const int K0 = e->cfg.k_max;
-  e->batched_kc = K0 >= 32 ? 32 : (K0 >= 16 ? 16 : 8);
-  e->batched_threads = 256;
-  const int bb = batched_blocks_per_sm(v, e->batched_kc, e->batched_threads);
+  if (K0 >= 64) e->shape = BatchedShape{32, 2, 256, 1};
+  else if (K0 >= 32) e->shape = BatchedShape{32, 1, 256, 1};
+  else if (K0 >= 16) e->shape = BatchedShape{16, 1, 256, 2};
+  else e->shape = BatchedShape{8, 1, 256, 2};
+  const int bb = batched_blocks_per_sm(v, e->shape);
   if (bb < 1) return fail(e, GW_ERR_CUDA, "batched kernel does not fit on an SM");
   e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bb * e->num_sms));
   GW_CUDA(e, cudaDeviceSynchronize());
@@ -1050,7 +1101,7 @@ static int launch_chain(gw_engine* e, const double* d_params, int K, double* d_s
   if (K == 1) {
     GW_CUDA(e, launch_plain(v, e->plain_grid, s));
   } else {
-    GW_CUDA(e, launch_batched(v, K, e->batched_kc, e->batched_threads, e->batched_grid, s));
+    GW_CUDA(e, launch_batched(v, K, e->shape, e->batched_grid, s));
   }
   if (ev_end) GW_CUDA(e, cudaEventRecord(ev_end, s));
   GW_CUDA(e, launch_bins_llh(v, K, d_sums, d_sums2, d_llh, d_llh_stat, s));
@@ -1165,46 +1216,43 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   std::vector<double> pts((size_t)K * e->cfg.n_params);
   for (size_t i = 0; i < pts.size(); ++i) pts[i] = 0.001 * (double)((i * 7919) % 17) - 0.008;
   GW_CUDA(e, cudaMemcpy(e->d_params, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice));
-  cudaEvent_t a, b;
+  cudaEvent_t a, b_ev;
   GW_CUDA(e, cudaEventCreate(&a));
-  GW_CUDA(e, cudaEventCreate(&b));
+  GW_CUDA(e, cudaEventCreate(&b_ev));
   float best = 1e30f;
-  int best_kc = e->batched_kc, best_th = e->batched_threads, best_grid = e->batched_grid;
-  const int kcs[3] = {8, 16, 32};
-  const int ths[2] = {128, 256};
-  for (int kc : kcs) {
-    if (kc > 8 && kc / 2 >= K) continue;  // wider passes than K waste lanes
-    for (int th : ths) {
-      const int bps = batched_blocks_per_sm(e->view, kc, th);
-      if (bps < 1) continue;
-      e->batched_kc = kc;
-      e->batched_threads = th;
-      e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
-      int rc = launch_chain(e, (const double*)e->d_params, K, (double*)e->d_sums, (double*)e->d_sums2,
-                            (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
-      if (rc) return rc;
-      GW_CUDA(e, cudaEventRecord(a, e->stream));
-      for (int rep = 0; rep < 3; ++rep) {
-        rc = launch_chain(e, (const double*)e->d_params, K, (double*)e->d_sums, (double*)e->d_sums2,
+  BatchedShape best_shape = e->shape;
+  int best_grid = e->batched_grid;
+  for (int i = 0; i < batched_shape_count(); ++i) {
+    const BatchedShape b = batched_shape(i);
+    const int per_pass = b.kc * b.kr;
+    if (b.kc > 8 && b.kc / 2 >= K) continue;    // lanes beyond K would idle
+    if (per_pass > 2 * ((K + 31) / 32) * 32) continue;
+    const int bps = batched_blocks_per_sm(e->view, b);
+    if (bps < 1) continue;
+    e->shape = b;
+    e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
+    int rc = launch_chain(e, (const double*)e->d_params, K, (double*)e->d_sums, (double*)e->d_sums2,
                           (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
-        if (rc) return rc;
-      }
-      GW_CUDA(e, cudaEventRecord(b, e->stream));
-      GW_CUDA(e, cudaEventSynchronize(b));
-      float ms = 0;
-      GW_CUDA(e, cudaEventElapsedTime(&ms, a, b));
-      if (ms < best) {
-        best = ms;
-        best_kc = kc;
-        best_th = th;
-        best_grid = e->batched_grid;
-      }
+    if (rc) return rc;
+    GW_CUDA(e, cudaEventRecord(a, e->stream));
+    for (int rep = 0; rep < 3; ++rep) {
+      rc = launch_chain(e, (const double*)e->d_params, K, (double*)e->d_sums, (double*)e->d_sums2,
+                        (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
+      if (rc) return rc;
+    }
+    GW_CUDA(e, cudaEventRecord(b_ev, e->stream));
+    GW_CUDA(e, cudaEventSynchronize(b_ev));
+    float ms = 0;
+    GW_CUDA(e, cudaEventElapsedTime(&ms, a, b_ev));
+    if (ms < best) {
+      best = ms;
+      best_shape = b;
+      best_grid = e->batched_grid;
     }
   }
   cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  e->batched_kc = best_kc;
-  e->batched_threads = best_th;
+  cudaEventDestroy(b_ev);
+  e->shape = best_shape;
   e->batched_grid = best_grid;
   e->tuned = true;
   for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
@@ -1212,10 +1260,11 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   return check_status(e);
 }
 
-extern "C" int gw_get_shape(const gw_engine* e, int32_t* kc, int32_t* threads) {
-  if (!e || !kc || !threads) return GW_ERR_ARG;
-  *kc = e->batched_kc;
-  *threads = e->batched_threads;
+extern "C" int gw_get_shape(const gw_engine* e, int32_t* kc, int32_t* threads, int32_t* stages) {
+  if (!e || !kc || !threads || !stages) return GW_ERR_ARG;
+  *kc = e->shape.kc * e->shape.kr;
+  *threads = e->shape.threads;
+  *stages = e->shape.stages;
   return GW_OK;
 }
 

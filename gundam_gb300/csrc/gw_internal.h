@@ -63,15 +63,22 @@ cudaError_t prepare_params(const DevView& v);  // once, before any launch or cap
 cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s);
 cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s);
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
-cudaError_t launch_batched(const DevView& v, int K, int kc, int threads, int grid, cudaStream_t s);
+// Shape of the batched kernel: kc points per warp pass, kr points per lane,
+// threads per block, payload stages.
+struct BatchedShape {
+  int kc, kr, threads, stages;
+};
+int batched_shape_count();
+BatchedShape batched_shape(int i);
+cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s);
 cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2, double* llh,
                             double* llh_stat, cudaStream_t s);
 
 // Shared memory a kernel shape needs, and how many CTAs fit on one SM.
 size_t plain_smem_bytes(const DevView& v);
-size_t batched_smem_bytes(const DevView& v, int kc, int threads);
+size_t batched_smem_bytes(const DevView& v, const BatchedShape& b);
 int plain_blocks_per_sm(const DevView& v);
-int batched_blocks_per_sm(const DevView& v, int kc, int threads);
+int batched_blocks_per_sm(const DevView& v, const BatchedShape& b);
 
 constexpr int kPlainThreads = 256;
 

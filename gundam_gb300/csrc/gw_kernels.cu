@@ -96,61 +96,106 @@ __device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned 
 }
 
 // ---------------------------------------------------------------------------
-// One dial.
+// One dial at KR parameter points (k0, k0 + kstep, ...): the header is
+// decoded, the type dispatched and the response clamp loaded once; the KR
+// evaluations are independent (instruction-level parallelism).
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T eval_dial(const DevView& v, uint64_t h, const T* __restrict__ pl, int k) {
+template <typename T, int KR>
+__device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const T* __restrict__ pl, int k0,
+                                            int kstep, T (&val)[KR]) {
   const int type = hdr_type(h);
   const int n = hdr_n(h);
   const T* d = pl + hdr_off(h);
   const int p0 = hdr_p0(h);
-  T val, lo, hi;
+  T lo, hi;
   if (type >= kTabulated) {
     // Tabulated.h:27-28 and Kriged.cpp:14-21; clamp of the table's dials.
     const TableDesc td = v.tables[p0];
     lo = (T)td.lower;
     hi = (T)td.upper;
-    const int64_t stride = td.per_k ? v.kpad : 1;
-    const T* tab = (const T*)v.table_arena + td.offset + (td.per_k ? k : 0);
-    if (type == kTabulated) {
-      const T f = d[0];
-      const int idx = (int)d[1];
-      val = f * tab[idx * stride] + (T(1) - f) * tab[(idx + 1) * stride];
-    } else {
-      val = T(0);
-      for (int j = 0; j < n; ++j) val += d[n + j] * tab[(int64_t)(int)d[j] * stride];
+    // per-point tables are laid out [entry][kpad]
+    const int64_t st = td.per_k ? v.kpad : 1;
+    const T* tab = (const T*)v.table_arena + td.offset;
+#pragma unroll
+    for (int j = 0; j < KR; ++j) {
+      const int64_t kk = td.per_k ? (int64_t)(k0 + j * kstep) : 0;
+      if (type == kTabulated) {
+        const T f = d[0];
+        const int idx = (int)d[1];
+        val[j] = f * tab[idx * st + kk] + (T(1) - f) * tab[(idx + 1) * st + kk];
+      } else {
+        T a = T(0);
+        for (int q = 0; q < n; ++q) a += d[n + q] * tab[(int64_t)(int)d[q] * st + kk];
+        val[j] = a;
+      }
     }
   } else {
-    const T* xs = (const T*)v.x;
-    const T x = xs[(size_t)p0 * v.kpad + k];
+    const T* xs = (const T*)v.x + (size_t)p0 * v.kpad + k0;
     const typename Vec2<T>::type c = ((const typename Vec2<T>::type*)v.pclamp)[p0];
     lo = c.x;
     hi = c.y;
     const bool trunc = (v.pflags[p0] & 1) != 0;
+    T x[KR];
+#pragma unroll
+    for (int j = 0; j < KR; ++j) x[j] = xs[j * kstep];
     switch (type) {
-      case kNorm: val = x; break;
-      case kMonotonic: val = eval_catmull<T, true>(d, n, x, trunc); break;
-      case kCompact: val = eval_catmull<T, false>(d, n, x, trunc); break;
-      case kUniform: val = eval_uniform<T>(d, n, x, trunc); break;
-      case kGeneral: val = eval_general<T>(d, n, x, trunc); break;
-      case kGraph: val = eval_graph<T>(d, n, x, trunc); break;
+      case kNorm:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = x[j];
+        break;
+      case kMonotonic:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
+          else val[j] = eval_catmull<T, true>(d, n, x[j], trunc);
+        }
+        break;
+      case kCompact:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
+          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
+        }
+        break;
+      case kUniform:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<false>(d, n, x[j], trunc);
+          else val[j] = eval_uniform<T>(d, n, x[j], trunc);
+        }
+        break;
+      case kGeneral:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
+        break;
+      case kGraph:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_graph<T>(d, n, x[j], trunc);
+        break;
       case kBilinear: {
-        const T y = xs[(size_t)hdr_p1(h) * v.kpad + k];
-        val = eval_bilinear<T>(d, x, y, trunc);
+        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
         break;
       }
       case kBicubic: {
-        const T y = xs[(size_t)hdr_p1(h) * v.kpad + k];
-        val = eval_bicubic<T>(d, x, y, trunc);
+        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], ys[j * kstep], trunc);
         break;
       }
-      default: return T(1);
+      default:
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = T(1);
+        return;
     }
   }
   // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
-  if (val < lo) val = lo;
-  else if (val > hi) val = hi;
-  return val;
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    if (val[j] < lo) val[j] = lo;
+    else if (val[j] > hi) val[j] = hi;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -286,7 +331,11 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int i = tid + j * kPlainThreads;
-      if (i < td.ndials) dval[hdr_slot(h[j])] = eval_dial<T>(v, h[j], pl, 0);
+      if (i < td.ndials) {
+        T val[1];
+        dial_values<T, 1>(v, h[j], pl, 0, 0, val);
+        dval[hdr_slot(h[j])] = val[0];
+      }
     }
     __syncthreads();
 
@@ -333,21 +382,22 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 // ---------------------------------------------------------------------------
 // K > 1: events in order, lanes = parameter points.  KC points share one
 // warp pass (32/KC events per pass); the tile payload is read from HBM once
-// for all K points.
+// for all K points.  ST = payload stages (2: the next tile's copy overlaps
+// this tile's work; 1: less shared memory, more resident CTAs).
 // ---------------------------------------------------------------------------
-template <typename T, int KC, int NT>
+template <typename T, int KC, int KR, int NT, int ST>
 __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
   constexpr int NW = NT / 32;
   constexpr int EPW = 32 / KC;
+  constexpr int KP = KC * KR;  // points per pass
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
   unsigned char* stage0 = smem;
-  unsigned char* stage1 = smem + TB;
-  uint64_t* shdr = (uint64_t*)(smem + 2 * TB);                    // [1024]
-  double2* wpart = (double2*)(shdr + 1024);                       // [8][NW][32]
-  T* sw0 = (T*)(wpart + kMaxLocalBins * NW * 32);                 // [256]
-  uint16_t* sinv = (uint16_t*)(sw0 + kMaxTileEvents);             // [1024]
-  uint16_t* sev = sinv + 1024;                                    // [257]
+  unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
+  uint64_t* shdr = (uint64_t*)(smem + ST * TB);               // [1024], indexed by slot
+  double2* wpart = (double2*)(shdr + 1024);                   // [lb][NW][KR][32]
+  T* sw0 = (T*)(wpart + kMaxLocalBins * NW * KR * 32);        // [256]
+  uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
   __shared__ uint64_t bar[2];
   __shared__ int s_present[kMaxLocalBins];
 
@@ -363,17 +413,16 @@ __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
   int tile = blockIdx.x;
   if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
   for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
-    const int st = it & 1;
-    const uint32_t parity = (uint32_t)((it >> 1) & 1);
+    const int st = (ST == 2) ? (it & 1) : 0;
+    const uint32_t parity = (ST == 2) ? (uint32_t)((it >> 1) & 1) : (uint32_t)(it & 1);
     const int next = tile + gridDim.x;
-    if (tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+    if (ST == 2 && tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
 
     const TileDesc td = v.tiles[tile];
     const int nd = td.ndials, ne = td.nevents;
     for (int i = tid; i < nd; i += NT) {
       const uint64_t h = v.hdr[td.dial0 + i];
-      shdr[i] = h;
-      sinv[hdr_slot(h)] = (uint16_t)i;
+      shdr[hdr_slot(h)] = h;
     }
     for (int e = tid; e < ne; e += NT) {
       sev[e] = v.evinfo[td.event0 + e];
@@ -385,7 +434,8 @@ __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicOr(v.status, kStatusCopyTimeout);
-        if (next < v.n_tiles) mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
+        if (ST == 2 && next < v.n_tiles)
+          mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
       }
       return;
     }
@@ -397,44 +447,67 @@ __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
     const int e_hi = min(ne, e_lo + chunk);
     const int sub = lane / KC, kl = lane % KC;
 
-    for (int kc = 0; kc < K; kc += KC) {
-      const int k = kc + kl;
+    for (int kb = 0; kb < K; kb += KP) {
+      const int k0 = kb + kl;  // this lane's points: k0 + j*KC
 #pragma unroll
-      for (int lb = 0; lb < kMaxLocalBins; ++lb) wpart[(lb * NW + warp) * 32 + lane] = make_double2(0.0, 0.0);
+      for (int lb = 0; lb < kMaxLocalBins; ++lb)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) wpart[((lb * NW + warp) * KR + j) * 32 + lane] = make_double2(0.0, 0.0);
       int cur = -1;
-      double s = 0.0, s2 = 0.0;
+      double s[KR], s2[KR];
+#pragma unroll
+      for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
       for (int base = e_lo; base < e_hi; base += EPW) {
         const int e = base + sub;
         if (e < e_hi) {
           const uint16_t ei = sev[e];
           const int s0 = ev_slot(ei), s1 = ev_slot(sev[e + 1]);
-          T w = T(1);
-          for (int sl = s0; sl < s1; ++sl) w *= eval_dial<T>(v, shdr[sinv[sl]], pl, k);
-          if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
-          w = sw0[e] * w;
+          T w[KR];
+#pragma unroll
+          for (int j = 0; j < KR; ++j) w[j] = T(1);
+          for (int sl = s0; sl < s1; ++sl) {
+            T val[KR];
+            dial_values<T, KR>(v, shdr[sl], pl, k0, KC, val);
+#pragma unroll
+            for (int j = 0; j < KR; ++j) w[j] *= val[j];
+          }
+          const T w0 = sw0[e];
           const int lb = ev_lbin(ei);
           if (lb != cur) {
-            if (cur >= 0) wpart[(cur * NW + warp) * 32 + lane] = make_double2(s, s2);
+            if (cur >= 0) {
+#pragma unroll
+              for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
+            }
             cur = lb;
-            s = 0.0;
-            s2 = 0.0;
+#pragma unroll
+            for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
           }
-          const double wd = (double)w;
-          s += wd;
-          s2 += wd * wd;
+#pragma unroll
+          for (int j = 0; j < KR; ++j) {
+            T wj = w[j];
+            if (v.has_cap && wj > (T)v.cap) wj = (T)v.cap;
+            wj = w0 * wj;
+            const double wd = (double)wj;
+            s[j] += wd;
+            s2[j] += wd * wd;
+          }
         }
       }
-      if (cur >= 0) wpart[(cur * NW + warp) * 32 + lane] = make_double2(s, s2);
+      if (cur >= 0) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
+      }
       __syncthreads();
-      for (int t = tid; t < kMaxLocalBins * KC; t += NT) {
-        const int lb = t / KC, kk = t % KC;
-        const int kg = kc + kk;
+      for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
+        const int lb = t / KP, r = t % KP;
+        const int j = r / KC, kk = r % KC;
+        const int kg = kb + kk + j * KC;
         if (kg < K && lb < (int)td.nbins && s_present[lb]) {
           double a = 0.0, a2 = 0.0;
           for (int w = 0; w < NW; ++w) {
 #pragma unroll
             for (int sb = 0; sb < EPW; ++sb) {
-              const double2 p = wpart[(lb * NW + w) * 32 + sb * KC + kk];
+              const double2 p = wpart[((lb * NW + w) * KR + j) * 32 + sb * KC + kk];
               a += p.x;
               a2 += p.y;
             }
@@ -445,6 +518,7 @@ __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
       }
       __syncthreads();
     }
+    if (ST == 1 && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
   }
 }
 
@@ -555,13 +629,12 @@ size_t plain_smem_bytes(const DevView& v) {
          kMaxTileEvents * sizeof(uint16_t);
 }
 
-size_t batched_smem_bytes(const DevView& v, int kc, int threads) {
-  (void)kc;
+size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
-  const int nw = threads / 32;
-  return 2 * (size_t)v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
-         (size_t)kMaxLocalBins * nw * 32 * sizeof(double2) + kMaxTileEvents * tsz +
-         1024 * sizeof(uint16_t) + (kMaxTileEvents + 1) * sizeof(uint16_t);
+  const int nw = b.threads / 32;
+  return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
+         (size_t)kMaxLocalBins * nw * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
+         (kMaxTileEvents + 1) * sizeof(uint16_t);
 }
 
 template <typename T>
@@ -569,24 +642,45 @@ static const void* plain_fn() {
   return (const void*)k_plain<T>;
 }
 
-template <typename T>
-static const void* batched_fn(int kc, int threads) {
-  if (threads == 128) {
-    if (kc == 8) return (const void*)k_batched<T, 8, 128>;
-    if (kc == 16) return (const void*)k_batched<T, 16, 128>;
-    return (const void*)k_batched<T, 32, 128>;
-  }
-  if (kc == 8) return (const void*)k_batched<T, 8, 256>;
-  if (kc == 16) return (const void*)k_batched<T, 16, 256>;
-  return (const void*)k_batched<T, 32, 256>;
+// The batched kernel shapes the autotuner chooses from.
+template <typename T, int KC, int KR, int NT, int ST>
+static void launch_b(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
+  k_batched<T, KC, KR, NT, ST><<<grid, NT, smem, s>>>(v, K);
+}
+
+struct ShapeEntry {
+  int kc, kr, threads, stages;
+  const void* fn[2];                                         // [double, float]
+  void (*launch[2])(const DevView&, int, int, size_t, cudaStream_t);
+};
+
+#define GW_SHAPE(KC, KR, NT, ST)                                                               \
+  {KC, KR, NT, ST, {(const void*)k_batched<double, KC, KR, NT, ST>,                           \
+                    (const void*)k_batched<float, KC, KR, NT, ST>},                            \
+   {launch_b<double, KC, KR, NT, ST>, launch_b<float, KC, KR, NT, ST>}}
+
+static const ShapeEntry kShapes[] = {
+    GW_SHAPE(8, 1, 256, 2),  GW_SHAPE(16, 1, 256, 2), GW_SHAPE(32, 1, 256, 2), GW_SHAPE(32, 1, 256, 1),
+    GW_SHAPE(32, 2, 256, 1), GW_SHAPE(32, 2, 256, 2), GW_SHAPE(32, 2, 128, 1), GW_SHAPE(32, 4, 128, 1),
+    GW_SHAPE(16, 2, 256, 1), GW_SHAPE(16, 2, 256, 2), GW_SHAPE(8, 2, 256, 2),  GW_SHAPE(32, 4, 256, 1),
+};
+#undef GW_SHAPE
+
+static const ShapeEntry* find_shape(const BatchedShape& b) {
+  for (const ShapeEntry& e : kShapes)
+    if (e.kc == b.kc && e.kr == b.kr && e.threads == b.threads && e.stages == b.stages) return &e;
+  return nullptr;
+}
+
+int batched_shape_count() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
+
+BatchedShape batched_shape(int i) {
+  const ShapeEntry& e = kShapes[i];
+  return BatchedShape{e.kc, e.kr, e.threads, e.stages};
 }
 
 static const void* pick_plain(const DevView& v) {
   return v.precision ? plain_fn<float>() : plain_fn<double>();
-}
-
-static const void* pick_batched(const DevView& v, int kc, int threads) {
-  return v.precision ? batched_fn<float>(kc, threads) : batched_fn<double>(kc, threads);
 }
 
 int plain_blocks_per_sm(const DevView& v) {
@@ -599,13 +693,20 @@ int plain_blocks_per_sm(const DevView& v) {
   return n;
 }
 
-int batched_blocks_per_sm(const DevView& v, int kc, int threads) {
-  const void* fn = pick_batched(v, kc, threads);
-  const size_t smem = batched_smem_bytes(v, kc, threads);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+int batched_blocks_per_sm(const DevView& v, const BatchedShape& b) {
+  const ShapeEntry* e = find_shape(b);
+  if (!e) return 0;
+  const void* fn = e->fn[v.precision ? 1 : 0];
+  const size_t smem = batched_smem_bytes(v, b);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
     return 0;
+  }
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, b.threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   return n;
 }
 
@@ -643,26 +744,10 @@ cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <typename T>
-static void launch_batched_t(const DevView& v, int K, int kc, int threads, int grid, size_t smem,
-                             cudaStream_t s) {
-  if (threads == 128) {
-    if (kc == 8) k_batched<T, 8, 128><<<grid, 128, smem, s>>>(v, K);
-    else if (kc == 16) k_batched<T, 16, 128><<<grid, 128, smem, s>>>(v, K);
-    else k_batched<T, 32, 128><<<grid, 128, smem, s>>>(v, K);
-  } else {
-    if (kc == 8) k_batched<T, 8, 256><<<grid, 256, smem, s>>>(v, K);
-    else if (kc == 16) k_batched<T, 16, 256><<<grid, 256, smem, s>>>(v, K);
-    else k_batched<T, 32, 256><<<grid, 256, smem, s>>>(v, K);
-  }
-}
-
-cudaError_t launch_batched(const DevView& v, int K, int kc, int threads, int grid, cudaStream_t s) {
-  const size_t smem = batched_smem_bytes(v, kc, threads);
-  if (v.precision)
-    launch_batched_t<float>(v, K, kc, threads, grid, smem, s);
-  else
-    launch_batched_t<double>(v, K, kc, threads, grid, smem, s);
+cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s) {
+  const ShapeEntry* e = find_shape(b);
+  if (!e) return cudaErrorInvalidValue;
+  e->launch[v.precision ? 1 : 0](v, K, grid, batched_smem_bytes(v, b), s);
   return cudaGetLastError();
 }
 

@@ -23,7 +23,7 @@ namespace gw {
 
 constexpr int kMaxTileDials = 1023;   // slot field is 10 bits
 constexpr int kMaxTileEvents = 256;   // one event per thread in the plain kernel
-constexpr int kMaxLocalBins = 8;      // bins spanned by one tile (bin - bin0 < 8)
+constexpr int kMaxLocalBins = 4;      // bins spanned by one tile (bin - bin0 < 4)
 constexpr int kMaxPayloadElems = 8191; // 13-bit element offset
 constexpr int kMaxKnots = 31;         // 5-bit count field
 constexpr int kTypeCount = 11;

@@ -147,9 +147,10 @@ class Engine:
     def autotune(self, K): self._chk(self.lib.gw_autotune(self._e, K))
 
     def shape(self):
-        a, b = C.c_int32(), C.c_int32()
-        self._chk(self.lib.gw_get_shape(self._e, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(points per warp pass, threads per block, payload stages) of the batched kernel."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._chk(self.lib.gw_get_shape(self._e, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def set_event_weight_copy(self, on=True): self._chk(self.lib.gw_set_event_weight_copy(self._e, int(on)))
 

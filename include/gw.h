@@ -218,11 +218,12 @@ int gw_sync(gw_engine* e);
 int gw_use_graph(gw_engine* e, int32_t on);
 
 /* Times the batched kernel shapes for K points and keeps the fastest
- * (points per warp pass x threads per block). */
+ * (points per warp pass x threads per block x payload stages). */
 int gw_autotune(gw_engine* e, int32_t K);
 
-/* Copies the chosen batched shape out (after gw_autotune). */
-int gw_get_shape(const gw_engine* e, int32_t* points_per_pass, int32_t* threads);
+/* Copies the batched shape in use out: parameter points per pass, threads per
+ * block, payload stages. */
+int gw_get_shape(const gw_engine* e, int32_t* points_per_pass, int32_t* threads, int32_t* stages);
 
 /* Cache::Manager::SetIsEventWeightCopyEnabled (CacheManager.h:119). */
 int gw_set_event_weight_copy(gw_engine* e, int32_t enable);
