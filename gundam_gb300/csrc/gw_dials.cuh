@@ -6,7 +6,7 @@
 // payload in shared memory.  The CPU dial wrappers call these with bounds
 // (-1e20, 1e20) and apply the collection's response clamp afterwards
 // (MonotonicSpline.cpp:71-84, DialResponseSupervisor.cpp:10-18); the engine
-// does the same.
+// applies both as one clamp after the call (gw_kernels.cu, dial_values).
 #pragma once
 #include "gw_layout.h"
 
@@ -16,14 +16,6 @@ namespace gw {
 // reciprocal-multiply form in FP32 mode (within the FP32 tolerance).
 __device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
-
-template <typename T>
-__device__ __forceinline__ T clamp_bounds(T v) {
-  const T lo = T(-1e20), hi = T(1e20);
-  if (v < lo) v = lo;
-  if (v > hi) v = hi;
-  return v;
-}
 
 // Hermite cubic on [p1, p2] with end slopes m1, m2 (already scaled by the
 // interval width), Horner form of CalculateUniformSpline.h:71-74.
@@ -76,7 +68,7 @@ __device__ __forceinline__ T eval_catmull(const T* __restrict__ d, int n, T x, b
   }
   const T v = ((((T(2) * p2 - T(2) * p3 + m3 + m2) * fx + T(3) * p3 - T(3) * p2 - m3 - T(2) * m2) * fx +
                 m2) * fx + p2);
-  return clamp_bounds(v);
+  return v;
 }
 
 // Hermite spline on uniform knots with stored slopes: CalculateUniformSpline.h:46-80.
@@ -100,7 +92,7 @@ __device__ __forceinline__ T eval_uniform(const T* __restrict__ d, int n, T x, b
   const T m1 = k[1] * step;
   const T p2 = k[2];
   const T m2 = k[3] * step;
-  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
+  return (hermite(p1, m1, p2, m2, fx));
 }
 
 // Hermite spline on non-uniform knots: CalculateGeneralSpline.h:51-197, with
@@ -128,7 +120,7 @@ __device__ __forceinline__ T eval_general(const T* __restrict__ d, int n, T x, b
   const T m1 = d[3 * ix + 1] * step;
   const T p2 = d[3 * (ix + 1)];
   const T m2 = d[3 * (ix + 1) + 1] * step;
-  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
+  return (hermite(p1, m1, p2, m2, fx));
 }
 
 // Piecewise-linear graph: CalculateGraph.h:43-88.  d = [(y, x) x n].
@@ -152,7 +144,7 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
   const T step = x2 - x1;
   const T fx = fdiv(x - x1, step);
   const T m = p2 - p1;
-  return clamp_bounds(p1 + fx * m);
+  return (p1 + fx * m);
 }
 
 // FP32 layout of the Catmull-Rom and uniform splines.  The host stores each
@@ -178,7 +170,7 @@ __device__ __forceinline__ float eval_prepared(const float* __restrict__ d, int 
     if (ix < 0) m2 = p2 - p1;
     if (ix > n - 2) m1 = p2 - p1;
   }
-  return clamp_bounds(hermite(p1, m1, p2, m2, fx));
+  return (hermite(p1, m1, p2, m2, fx));
 }
 
 // Index of the facet for a value: BilinearIndex / BicubicIndex
@@ -217,7 +209,7 @@ __device__ __forceinline__ T eval_bilinear(const T* __restrict__ d, T x, T y, bo
   const int iy = surface_index(y, yy, ny - 1);
   const T v0 = lin(x, xx[ix], z[ix * ny + iy], xx[ix + 1], z[(ix + 1) * ny + iy]);
   const T v1 = lin(x, xx[ix], z[ix * ny + iy + 1], xx[ix + 1], z[(ix + 1) * ny + iy + 1]);
-  return clamp_bounds(lin(y, yy[iy], v0, yy[iy + 1], v1));
+  return (lin(y, yy[iy], v0, yy[iy + 1], v1));
 }
 
 // One Catmull-Rom segment through (x0,p0)..(x3,p3) evaluated between x1 and
@@ -283,7 +275,7 @@ __device__ __forceinline__ T eval_bicubic(const T* __restrict__ d, T x, T y, boo
     v[r] = cubic_seg(x, a0, surf_knot(z, nx, ny, ix - 1, j), a1, surf_knot(z, nx, ny, ix, j), a2,
                      surf_knot(z, nx, ny, ix + 1, j), a3, surf_knot(z, nx, ny, ix + 2, j));
   }
-  return clamp_bounds(cubic_seg(y, u[0], v[0], u[1], v[1], u[2], v[2], u[3], v[3]));
+  return (cubic_seg(y, u[0], v[0], u[1], v[1], u[2], v[2], u[3], v[3]));
 }
 
 }  // namespace gw

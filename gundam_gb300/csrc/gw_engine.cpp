@@ -656,6 +656,14 @@ int build_and_upload(gw_engine* e) {
   // 1. every result needs a bin (CacheManager.cpp:727-729 "Histogram cells are missing")
   for (int r = 0; r < N; ++r)
     if (e->bin[r] < 0) return fail(e, GW_ERR_STATE, "result %d has no histogram bin", r);
+  // response clamps must be ordered (the kernels apply them as one interval)
+  for (int p = 0; p < e->cfg.n_params; ++p)
+    if (!(e->clamp_lo[p] <= e->clamp_hi[p]))
+      return fail(e, GW_ERR_ARG, "parameter %d: lower clamp %g above upper clamp %g", p, e->clamp_lo[p],
+                  e->clamp_hi[p]);
+  for (size_t t = 0; t < e->tables.size(); ++t)
+    if (!(e->tables[t].lower <= e->tables[t].upper))
+      return fail(e, GW_ERR_ARG, "table %zu: lower clamp above upper clamp", t);
 
   // 2. dials grouped by result, insertion order kept (counting sort)
   std::vector<int64_t> rstart((size_t)N + 1, 0);

@@ -138,56 +138,52 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
     T x[KR];
 #pragma unroll
     for (int j = 0; j < KR; ++j) x[j] = xs[j * kstep];
-    switch (type) {
-      case kNorm:
+    if (type == kNorm) {
 #pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = x[j];
-        break;
-      case kMonotonic:
+      for (int j = 0; j < KR; ++j) val[j] = x[j];
+    } else {
+      // Spline, graph and surface responses: Calculate*.h clamps to
+      // [-1e20, 1e20] before the response clamp; with lower <= upper the two
+      // clamps are one clamp to the intersection.
+      if (lo < T(-1e20)) lo = T(-1e20);
+      if (hi > T(1e20)) hi = T(1e20);
+      if (type == kMonotonic) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) {
           if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
           else val[j] = eval_catmull<T, true>(d, n, x[j], trunc);
         }
-        break;
-      case kCompact:
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
-          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
-        }
-        break;
-      case kUniform:
+      } else if (type == kUniform) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) {
           if constexpr (sizeof(T) == 4) val[j] = eval_prepared<false>(d, n, x[j], trunc);
           else val[j] = eval_uniform<T>(d, n, x[j], trunc);
         }
-        break;
-      case kGeneral:
+      } else if (type == kGeneral) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
-        break;
-      case kGraph:
+      } else if (type == kGraph) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_graph<T>(d, n, x[j], trunc);
-        break;
-      case kBilinear: {
+      } else if (type == kBilinear) {
         const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
-        break;
-      }
-      case kBicubic: {
+      } else if (type == kCompact) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
+          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
+        }
+      } else if (type == kBicubic) {
         const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], ys[j * kstep], trunc);
-        break;
-      }
-      default:
+      } else {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = T(1);
         return;
+      }
     }
   }
   // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
@@ -442,9 +438,20 @@ __global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
     for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
     const T* pl = (const T*)(st ? stage1 : stage0);
 
-    const int chunk = (ne + NW - 1) / NW;
-    const int e_lo = warp * chunk;
-    const int e_hi = min(ne, e_lo + chunk);
+    // Each warp takes a contiguous run of events holding ~nd/NW dials: the
+    // first event whose first slot reaches warp*nd/NW (a fixed, deterministic
+    // split, so the FP64 summation order does not depend on scheduling).
+    auto first_event_at = [&](int target) {
+      int lo = 0, hi = ne;  // sev[ne] holds nd
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ev_slot(sev[mid]) < target) lo = mid + 1;
+        else hi = mid;
+      }
+      return lo;
+    };
+    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * nd) / NW);
+    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * nd) / NW);
     const int sub = lane / KC, kl = lane % KC;
 
     for (int kb = 0; kb < K; kb += KP) {
