@@ -266,6 +266,7 @@ def run_gw(args, world, rank, local, dist):
         if key in tr:
             traffic = tr[key]
     layout = eng.layout()
+    shape = eng.shape()
     variants = {}
     if not args.no_variants:
         # the same engine at K=1 (plain kernel), and the FP64 engine at K=1
@@ -303,10 +304,13 @@ def run_gw(args, world, rank, local, dist):
                                    f"{wl.n_bins} bins, {wl.n_params} params",
                        "points_per_step": K, "precision": args.precision, "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}", "tiles": layout["n_tiles"],
-                       "payload_bytes": layout["payload_bytes"]},
+                       "payload_bytes": layout["payload_bytes"],
+                       "kernel_shape": {"family": shape[0], "points_per_pass": shape[1], "threads": shape[2],
+                                        "stages": shape[3]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_batched" if K > 1 else "k_plain", "kernel_ms": kernel_ms,
+                         "kernel": ("k_plain" if K == 1 else ("k_multi" if shape[0] == 1 else "k_batched")),
+                         "kernel_ms": kernel_ms,
                          "algorithmic_bytes_per_launch": alg},
             "cpu_baseline": cpu,
             "e2e": e2e,

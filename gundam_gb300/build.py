@@ -72,11 +72,10 @@ def build(verbose: bool = False) -> dict[str, Path]:
     cxx = os.environ.get("CXX", "g++")
 
     common_nv = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
-    k_obj = objdir / "gw_kernels.o"
-    e_obj = objdir / "gw_engine.o"
-    jobs = [
-        ("gw_kernels", [nvcc, *common_nv, "-c", str(CSRC / "gw_kernels.cu"), "-o", str(k_obj)]),
-        ("gw_engine", [nvcc, *common_nv, "-c", str(CSRC / "gw_engine.cpp"), "-o", str(e_obj)]),
+    units = ["gw_kernels.cu", "gw_lanes.cu", "gw_multi.cu", "gw_engine.cpp"]
+    objs = [objdir / (Path(u).stem + ".o") for u in units]
+    jobs = [(u, [nvcc, *common_nv, "-c", str(CSRC / u), "-o", str(o)]) for u, o in zip(units, objs)]
+    jobs += [
         (
             "gw_workload",
             [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", "-I", str(INCLUDE),
@@ -94,7 +93,7 @@ def build(verbose: bool = False) -> dict[str, Path]:
         jobs.append(("ref_dials", [sys.executable, str(ref_script), str(reference)]))
     _run_all(jobs, verbose)
     link = [
-        nvcc, *ARCH, "-shared", "-cudart", "shared", str(k_obj), str(e_obj), "-o", str(LIBDIR / "libgw.so"),
+        nvcc, *ARCH, "-shared", "-cudart", "shared", *[str(o) for o in objs], "-o", str(LIBDIR / "libgw.so"),
         "-Xlinker", f"-rpath,{cudalib}", "-L", cudalib, "-lcudart",
     ]
     _run_all([("link libgw", link)], verbose)

@@ -1,0 +1,185 @@
+// gw_device.cuh -- device helpers shared by the kernel translation units:
+// bulk-copy (TMA) + mbarrier primitives with bounded waits, and the
+// multi-point dial evaluation used by every reweighting kernel.
+#pragma once
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "gw_dials.cuh"
+#include "gw_internal.h"
+
+namespace gw {
+namespace {
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+// ---------------------------------------------------------------------------
+// Bulk-copy (TMA) and mbarrier helpers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the barrier phase; gives up (returns false) after limit_ns.
+__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per tile copy
+
+// Thread 0: start the bulk copy of a tile's payload into a stage buffer.
+__device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned char* buf, uint64_t* bar) {
+  const TileDesc td = v.tiles[tile];
+  const uint32_t bytes = (uint32_t)td.payload_16b * 16u;
+  mbar_expect_tx(bar, bytes);
+  if (bytes > 0) bulk_load(buf, v.payload + td.payload_off, bytes, bar);
+}
+
+// ---------------------------------------------------------------------------
+// One dial at KR parameter points (k0, k0 + kstep, ...): the header is
+// decoded, the type dispatched and the response clamp loaded once; the KR
+// evaluations are independent (instruction-level parallelism).
+// ---------------------------------------------------------------------------
+template <typename T, int KR>
+__device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const T* __restrict__ pl, int k0,
+                                            int kstep, T (&val)[KR]) {
+  const int type = hdr_type(h);
+  const int n = hdr_n(h);
+  const T* d = pl + hdr_off(h);
+  const int p0 = hdr_p0(h);
+  T lo, hi;
+  if (type >= kTabulated) {
+    // Tabulated.h:27-28 and Kriged.cpp:14-21; clamp of the table's dials.
+    const TableDesc td = v.tables[p0];
+    lo = (T)td.lower;
+    hi = (T)td.upper;
+    // per-point tables are laid out [entry][kpad]
+    const int64_t st = td.per_k ? v.kpad : 1;
+    const T* tab = (const T*)v.table_arena + td.offset;
+#pragma unroll
+    for (int j = 0; j < KR; ++j) {
+      const int64_t kk = td.per_k ? (int64_t)(k0 + j * kstep) : 0;
+      if (type == kTabulated) {
+        const T f = d[0];
+        const int idx = (int)d[1];
+        val[j] = f * tab[idx * st + kk] + (T(1) - f) * tab[(idx + 1) * st + kk];
+      } else {
+        T a = T(0);
+        for (int q = 0; q < n; ++q) a += d[n + q] * tab[(int64_t)(int)d[q] * st + kk];
+        val[j] = a;
+      }
+    }
+  } else {
+    const T* xs = (const T*)v.x + (size_t)p0 * v.kpad + k0;
+    const typename Vec2<T>::type c = ((const typename Vec2<T>::type*)v.pclamp)[p0];
+    lo = c.x;
+    hi = c.y;
+    const bool trunc = (v.pflags[p0] & 1) != 0;
+    T x[KR];
+#pragma unroll
+    for (int j = 0; j < KR; ++j) x[j] = xs[j * kstep];
+    if (type == kNorm) {
+#pragma unroll
+      for (int j = 0; j < KR; ++j) val[j] = x[j];
+    } else {
+      // Spline, graph and surface responses: Calculate*.h clamps to
+      // [-1e20, 1e20] before the response clamp; with lower <= upper the two
+      // clamps are one clamp to the intersection.
+      if (lo < T(-1e20)) lo = T(-1e20);
+      if (hi > T(1e20)) hi = T(1e20);
+      if (type == kMonotonic) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
+          else val[j] = eval_catmull<T, true>(d, n, x[j], trunc);
+        }
+      } else if (type == kUniform) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<false>(d, n, x[j], trunc);
+          else val[j] = eval_uniform<T>(d, n, x[j], trunc);
+        }
+      } else if (type == kGeneral) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
+      } else if (type == kGraph) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_graph<T>(d, n, x[j], trunc);
+      } else if (type == kBilinear) {
+        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
+      } else if (type == kCompact) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
+          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
+        }
+      } else if (type == kBicubic) {
+        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], ys[j * kstep], trunc);
+      } else {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) val[j] = T(1);
+        return;
+      }
+    }
+  }
+  // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    if (val[j] < lo) val[j] = lo;
+    else if (val[j] > hi) val[j] = hi;
+  }
+}
+
+}  // namespace
+}  // namespace gw

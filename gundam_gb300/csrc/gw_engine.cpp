@@ -93,7 +93,7 @@ struct gw_engine {
   int kpad = 32;
   int n_slots = 0;
   int plain_grid = 1;
-  BatchedShape shape{32, 2, 256, 1};
+  BatchedShape shape{0, 32, 2, 256, 1};
   int batched_grid = 1;
   bool tuned = false;
   int max_fn_table = 0;
@@ -1029,10 +1029,8 @@ int build_and_upload(gw_engine* e) {
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
   e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bps * e->num_sms));
   const int K0 = e->cfg.k_max;
-  if (K0 >= 64) e->shape = BatchedShape{32, 2, 256, 1};
-  else if (K0 >= 32) e->shape = BatchedShape{32, 1, 256, 1};
-  else if (K0 >= 16) e->shape = BatchedShape{16, 1, 256, 2};
-  else e->shape = BatchedShape{8, 1, 256, 2};
+  if (K0 >= 8) e->shape = BatchedShape{1, 8, 4, 256, 1};
+  else e->shape = BatchedShape{1, 4, 2, 256, 2};
   const int bb = batched_blocks_per_sm(v, e->shape);
   if (bb < 1) return fail(e, GW_ERR_CUDA, "batched kernel does not fit on an SM");
   e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bb * e->num_sms));
@@ -1232,9 +1230,12 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   int best_grid = e->batched_grid;
   for (int i = 0; i < batched_shape_count(); ++i) {
     const BatchedShape b = batched_shape(i);
-    const int per_pass = b.kc * b.kr;
-    if (b.kc > 8 && b.kc / 2 >= K) continue;    // lanes beyond K would idle
-    if (per_pass > 2 * ((K + 31) / 32) * 32) continue;
+    if (b.kind == 0) {
+      if (b.kc > 8 && b.kc / 2 >= K) continue;  // lanes beyond K would idle
+      if (b.kc * b.kr > 2 * ((K + 31) / 32) * 32) continue;
+    } else if (b.kc > 2 * K) {
+      continue;
+    }
     const int bps = batched_blocks_per_sm(e->view, b);
     if (bps < 1) continue;
     e->shape = b;
@@ -1268,9 +1269,10 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   return check_status(e);
 }
 
-extern "C" int gw_get_shape(const gw_engine* e, int32_t* kc, int32_t* threads, int32_t* stages) {
-  if (!e || !kc || !threads || !stages) return GW_ERR_ARG;
-  *kc = e->shape.kc * e->shape.kr;
+extern "C" int gw_get_shape(const gw_engine* e, int32_t* kind, int32_t* kc, int32_t* threads, int32_t* stages) {
+  if (!e || !kind || !kc || !threads || !stages) return GW_ERR_ARG;
+  *kind = e->shape.kind;
+  *kc = e->shape.kind == 0 ? e->shape.kc * e->shape.kr : e->shape.kc;
   *threads = e->shape.threads;
   *stages = e->shape.stages;
   return GW_OK;

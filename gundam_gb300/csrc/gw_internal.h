@@ -63,13 +63,25 @@ cudaError_t prepare_params(const DevView& v);  // once, before any launch or cap
 cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s);
 cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s);
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
-// Shape of the batched kernel: kc points per warp pass, kr points per lane,
-// threads per block, payload stages.
+// Shape of a batched (K > 1) launch.  kind 0 = k_batched: lanes over points,
+// kc points per warp pass, kr points per lane.  kind 1 = k_multi: threads over
+// dials, kc points per chunk, kr points per thread.  threads per block and
+// payload stages for both.
 struct BatchedShape {
-  int kc, kr, threads, stages;
+  int kind, kc, kr, threads, stages;
 };
 int batched_shape_count();
 BatchedShape batched_shape(int i);
+
+// One compiled batched kernel: its function (for occupancy queries) and its
+// launcher, per precision [FP64, FP32].
+struct ShapeEntry {
+  int kind, kc, kr, threads, stages;
+  const void* fn[2];
+  void (*launch[2])(const DevView&, int, int, size_t, cudaStream_t);
+};
+int lane_shapes(const ShapeEntry** out);   // gw_lanes.cu
+int multi_shapes(const ShapeEntry** out);  // gw_multi.cu
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s);
 cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2, double* llh,
                             double* llh_stat, cudaStream_t s);

@@ -15,184 +15,10 @@
 //               and reduce it, deterministically, to one value per point.
 // The reference needs ~1 + n_types + 2*(2 + log2 max bin occupancy) launches
 // for the same work (CacheWeights.cpp:153-183, CacheRecursiveSums.cpp:282-352).
-#include <cfloat>
-#include <cmath>
-#include <cstdint>
-
-#include "gw_dials.cuh"
-#include "gw_internal.h"
+#include "gw_device.cuh"
 
 namespace gw {
 namespace {
-
-template <typename T> struct Vec2;
-template <> struct Vec2<double> { using type = double2; };
-template <> struct Vec2<float> { using type = float2; };
-
-// ---------------------------------------------------------------------------
-// Bulk-copy (TMA) and mbarrier helpers.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Waits for the barrier phase; gives up (returns false) after limit_ns.
-__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  for (;;) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > limit_ns) return false;
-  }
-}
-
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per tile copy
-
-// Thread 0: start the bulk copy of a tile's payload into a stage buffer.
-__device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned char* buf, uint64_t* bar) {
-  const TileDesc td = v.tiles[tile];
-  const uint32_t bytes = (uint32_t)td.payload_16b * 16u;
-  mbar_expect_tx(bar, bytes);
-  if (bytes > 0) bulk_load(buf, v.payload + td.payload_off, bytes, bar);
-}
-
-// ---------------------------------------------------------------------------
-// One dial at KR parameter points (k0, k0 + kstep, ...): the header is
-// decoded, the type dispatched and the response clamp loaded once; the KR
-// evaluations are independent (instruction-level parallelism).
-// ---------------------------------------------------------------------------
-template <typename T, int KR>
-__device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const T* __restrict__ pl, int k0,
-                                            int kstep, T (&val)[KR]) {
-  const int type = hdr_type(h);
-  const int n = hdr_n(h);
-  const T* d = pl + hdr_off(h);
-  const int p0 = hdr_p0(h);
-  T lo, hi;
-  if (type >= kTabulated) {
-    // Tabulated.h:27-28 and Kriged.cpp:14-21; clamp of the table's dials.
-    const TableDesc td = v.tables[p0];
-    lo = (T)td.lower;
-    hi = (T)td.upper;
-    // per-point tables are laid out [entry][kpad]
-    const int64_t st = td.per_k ? v.kpad : 1;
-    const T* tab = (const T*)v.table_arena + td.offset;
-#pragma unroll
-    for (int j = 0; j < KR; ++j) {
-      const int64_t kk = td.per_k ? (int64_t)(k0 + j * kstep) : 0;
-      if (type == kTabulated) {
-        const T f = d[0];
-        const int idx = (int)d[1];
-        val[j] = f * tab[idx * st + kk] + (T(1) - f) * tab[(idx + 1) * st + kk];
-      } else {
-        T a = T(0);
-        for (int q = 0; q < n; ++q) a += d[n + q] * tab[(int64_t)(int)d[q] * st + kk];
-        val[j] = a;
-      }
-    }
-  } else {
-    const T* xs = (const T*)v.x + (size_t)p0 * v.kpad + k0;
-    const typename Vec2<T>::type c = ((const typename Vec2<T>::type*)v.pclamp)[p0];
-    lo = c.x;
-    hi = c.y;
-    const bool trunc = (v.pflags[p0] & 1) != 0;
-    T x[KR];
-#pragma unroll
-    for (int j = 0; j < KR; ++j) x[j] = xs[j * kstep];
-    if (type == kNorm) {
-#pragma unroll
-      for (int j = 0; j < KR; ++j) val[j] = x[j];
-    } else {
-      // Spline, graph and surface responses: Calculate*.h clamps to
-      // [-1e20, 1e20] before the response clamp; with lower <= upper the two
-      // clamps are one clamp to the intersection.
-      if (lo < T(-1e20)) lo = T(-1e20);
-      if (hi > T(1e20)) hi = T(1e20);
-      if (type == kMonotonic) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
-          else val[j] = eval_catmull<T, true>(d, n, x[j], trunc);
-        }
-      } else if (type == kUniform) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<false>(d, n, x[j], trunc);
-          else val[j] = eval_uniform<T>(d, n, x[j], trunc);
-        }
-      } else if (type == kGeneral) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
-      } else if (type == kGraph) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_graph<T>(d, n, x[j], trunc);
-      } else if (type == kBilinear) {
-        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
-#pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
-      } else if (type == kCompact) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
-          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
-        }
-      } else if (type == kBicubic) {
-        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
-#pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], ys[j * kstep], trunc);
-      } else {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = T(1);
-        return;
-      }
-    }
-  }
-  // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
-#pragma unroll
-  for (int j = 0; j < KR; ++j) {
-    if (val[j] < lo) val[j] = lo;
-    else if (val[j] > hi) val[j] = hi;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Parameter update: mirror into the dial inputs, prior penalty.
@@ -376,160 +202,6 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 }
 
 // ---------------------------------------------------------------------------
-// K > 1: events in order, lanes = parameter points.  KC points share one
-// warp pass (32/KC events per pass); the tile payload is read from HBM once
-// for all K points.  ST = payload stages (2: the next tile's copy overlaps
-// this tile's work; 1: less shared memory, more resident CTAs).
-// ---------------------------------------------------------------------------
-template <typename T, int KC, int KR, int NT, int ST>
-__global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
-  constexpr int NW = NT / 32;
-  constexpr int EPW = 32 / KC;
-  constexpr int KP = KC * KR;  // points per pass
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int TB = v.tile_payload_bytes;
-  unsigned char* stage0 = smem;
-  unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
-  uint64_t* shdr = (uint64_t*)(smem + ST * TB);               // [1024], indexed by slot
-  double2* wpart = (double2*)(shdr + 1024);                   // [lb][NW][KR][32]
-  T* sw0 = (T*)(wpart + kMaxLocalBins * NW * KR * 32);        // [256]
-  uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
-  __shared__ uint64_t bar[2];
-  __shared__ int s_present[kMaxLocalBins];
-
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-
-  int tile = blockIdx.x;
-  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
-  for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
-    const int st = (ST == 2) ? (it & 1) : 0;
-    const uint32_t parity = (ST == 2) ? (uint32_t)((it >> 1) & 1) : (uint32_t)(it & 1);
-    const int next = tile + gridDim.x;
-    if (ST == 2 && tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
-
-    const TileDesc td = v.tiles[tile];
-    const int nd = td.ndials, ne = td.nevents;
-    for (int i = tid; i < nd; i += NT) {
-      const uint64_t h = v.hdr[td.dial0 + i];
-      shdr[hdr_slot(h)] = h;
-    }
-    for (int e = tid; e < ne; e += NT) {
-      sev[e] = v.evinfo[td.event0 + e];
-      sw0[e] = ((const T*)v.w0)[td.event0 + e];
-    }
-    if (tid == 0) sev[ne] = make_evinfo(nd, 0);
-    if (tid < kMaxLocalBins) s_present[tid] = 0;
-    const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) {
-        atomicOr(v.status, kStatusCopyTimeout);
-        if (ST == 2 && next < v.n_tiles)
-          mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
-      }
-      return;
-    }
-    for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
-    const T* pl = (const T*)(st ? stage1 : stage0);
-
-    // Each warp takes a contiguous run of events holding ~nd/NW dials: the
-    // first event whose first slot reaches warp*nd/NW (a fixed, deterministic
-    // split, so the FP64 summation order does not depend on scheduling).
-    auto first_event_at = [&](int target) {
-      int lo = 0, hi = ne;  // sev[ne] holds nd
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (ev_slot(sev[mid]) < target) lo = mid + 1;
-        else hi = mid;
-      }
-      return lo;
-    };
-    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * nd) / NW);
-    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * nd) / NW);
-    const int sub = lane / KC, kl = lane % KC;
-
-    for (int kb = 0; kb < K; kb += KP) {
-      const int k0 = kb + kl;  // this lane's points: k0 + j*KC
-#pragma unroll
-      for (int lb = 0; lb < kMaxLocalBins; ++lb)
-#pragma unroll
-        for (int j = 0; j < KR; ++j) wpart[((lb * NW + warp) * KR + j) * 32 + lane] = make_double2(0.0, 0.0);
-      int cur = -1;
-      double s[KR], s2[KR];
-#pragma unroll
-      for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
-      for (int base = e_lo; base < e_hi; base += EPW) {
-        const int e = base + sub;
-        if (e < e_hi) {
-          const uint16_t ei = sev[e];
-          const int s0 = ev_slot(ei), s1 = ev_slot(sev[e + 1]);
-          T w[KR];
-#pragma unroll
-          for (int j = 0; j < KR; ++j) w[j] = T(1);
-          for (int sl = s0; sl < s1; ++sl) {
-            T val[KR];
-            dial_values<T, KR>(v, shdr[sl], pl, k0, KC, val);
-#pragma unroll
-            for (int j = 0; j < KR; ++j) w[j] *= val[j];
-          }
-          const T w0 = sw0[e];
-          const int lb = ev_lbin(ei);
-          if (lb != cur) {
-            if (cur >= 0) {
-#pragma unroll
-              for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
-            }
-            cur = lb;
-#pragma unroll
-            for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
-          }
-#pragma unroll
-          for (int j = 0; j < KR; ++j) {
-            T wj = w[j];
-            if (v.has_cap && wj > (T)v.cap) wj = (T)v.cap;
-            wj = w0 * wj;
-            const double wd = (double)wj;
-            s[j] += wd;
-            s2[j] += wd * wd;
-          }
-        }
-      }
-      if (cur >= 0) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
-      }
-      __syncthreads();
-      for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
-        const int lb = t / KP, r = t % KP;
-        const int j = r / KC, kk = r % KC;
-        const int kg = kb + kk + j * KC;
-        if (kg < K && lb < (int)td.nbins && s_present[lb]) {
-          double a = 0.0, a2 = 0.0;
-          for (int w = 0; w < NW; ++w) {
-#pragma unroll
-            for (int sb = 0; sb < EPW; ++sb) {
-              const double2 p = wpart[((lb * NW + w) * KR + j) * 32 + sb * KC + kk];
-              a += p.x;
-              a2 += p.y;
-            }
-          }
-          const int slot = (lb == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + lb];
-          v.partials[(size_t)slot * v.kpad + kg] = make_double2(a, a2);
-        }
-      }
-      __syncthreads();
-    }
-    if (ST == 1 && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Bin sums and likelihood.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double llh_poisson(double data, double pred) {
@@ -638,6 +310,11 @@ size_t plain_smem_bytes(const DevView& v) {
 
 size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  if (b.kind == 1) {  // k_multi
+    return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
+           (size_t)kMaxTileEvents * b.kc * sizeof(double) + (size_t)1024 * b.kc * tsz + kMaxTileEvents * tsz +
+           (kMaxTileEvents + 1) * sizeof(uint16_t);
+  }
   const int nw = b.threads / 32;
   return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
          (size_t)kMaxLocalBins * nw * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
@@ -649,41 +326,34 @@ static const void* plain_fn() {
   return (const void*)k_plain<T>;
 }
 
-// The batched kernel shapes the autotuner chooses from.
-template <typename T, int KC, int KR, int NT, int ST>
-static void launch_b(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
-  k_batched<T, KC, KR, NT, ST><<<grid, NT, smem, s>>>(v, K);
+// Every batched shape: the lanes-over-points family (gw_lanes.cu), then the
+// dials-over-threads family (gw_multi.cu).
+static const ShapeEntry* shape_entry(int i) {
+  const ShapeEntry* lanes;
+  const ShapeEntry* multi;
+  const int nl = lane_shapes(&lanes);
+  const int nm = multi_shapes(&multi);
+  if (i < 0 || i >= nl + nm) return nullptr;
+  return i < nl ? &lanes[i] : &multi[i - nl];
 }
 
-struct ShapeEntry {
-  int kc, kr, threads, stages;
-  const void* fn[2];                                         // [double, float]
-  void (*launch[2])(const DevView&, int, int, size_t, cudaStream_t);
-};
-
-#define GW_SHAPE(KC, KR, NT, ST)                                                               \
-  {KC, KR, NT, ST, {(const void*)k_batched<double, KC, KR, NT, ST>,                           \
-                    (const void*)k_batched<float, KC, KR, NT, ST>},                            \
-   {launch_b<double, KC, KR, NT, ST>, launch_b<float, KC, KR, NT, ST>}}
-
-static const ShapeEntry kShapes[] = {
-    GW_SHAPE(8, 1, 256, 2),  GW_SHAPE(16, 1, 256, 2), GW_SHAPE(32, 1, 256, 2), GW_SHAPE(32, 1, 256, 1),
-    GW_SHAPE(32, 2, 256, 1), GW_SHAPE(32, 2, 256, 2), GW_SHAPE(32, 2, 128, 1), GW_SHAPE(32, 4, 128, 1),
-    GW_SHAPE(16, 2, 256, 1), GW_SHAPE(16, 2, 256, 2), GW_SHAPE(8, 2, 256, 2),  GW_SHAPE(32, 4, 256, 1),
-};
-#undef GW_SHAPE
-
-static const ShapeEntry* find_shape(const BatchedShape& b) {
-  for (const ShapeEntry& e : kShapes)
-    if (e.kc == b.kc && e.kr == b.kr && e.threads == b.threads && e.stages == b.stages) return &e;
-  return nullptr;
+int batched_shape_count() {
+  const ShapeEntry* p;
+  return lane_shapes(&p) + multi_shapes(&p);
 }
-
-int batched_shape_count() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
 
 BatchedShape batched_shape(int i) {
-  const ShapeEntry& e = kShapes[i];
-  return BatchedShape{e.kc, e.kr, e.threads, e.stages};
+  const ShapeEntry& e = *shape_entry(i);
+  return BatchedShape{e.kind, e.kc, e.kr, e.threads, e.stages};
+}
+
+static const ShapeEntry* find_shape(const BatchedShape& b) {
+  for (int i = 0; i < batched_shape_count(); ++i) {
+    const ShapeEntry* e = shape_entry(i);
+    if (e->kind == b.kind && e->kc == b.kc && e->kr == b.kr && e->threads == b.threads && e->stages == b.stages)
+      return e;
+  }
+  return nullptr;
 }
 
 static const void* pick_plain(const DevView& v) {

@@ -1,0 +1,186 @@
+// gw_lanes.cu -- K > 1 reweighting kernel with lanes over parameter points
+// (one warp evaluates one dial for up to 32*KR points at once).
+#include "gw_device.cuh"
+
+namespace gw {
+namespace {
+
+// ---------------------------------------------------------------------------
+// K > 1: events in order, lanes = parameter points.  KC points share one
+// warp pass (32/KC events per pass); the tile payload is read from HBM once
+// for all K points.  ST = payload stages (2: the next tile's copy overlaps
+// this tile's work; 1: less shared memory, more resident CTAs).
+// ---------------------------------------------------------------------------
+template <typename T, int KC, int KR, int NT, int ST>
+__global__ void __launch_bounds__(NT) k_batched(const DevView v, int K) {
+  constexpr int NW = NT / 32;
+  constexpr int EPW = 32 / KC;
+  constexpr int KP = KC * KR;  // points per pass
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int TB = v.tile_payload_bytes;
+  unsigned char* stage0 = smem;
+  unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
+  uint64_t* shdr = (uint64_t*)(smem + ST * TB);               // [1024], indexed by slot
+  double2* wpart = (double2*)(shdr + 1024);                   // [lb][NW][KR][32]
+  T* sw0 = (T*)(wpart + kMaxLocalBins * NW * KR * 32);        // [256]
+  uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
+  __shared__ uint64_t bar[2];
+  __shared__ int s_present[kMaxLocalBins];
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int tile = blockIdx.x;
+  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
+  for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
+    const int st = (ST == 2) ? (it & 1) : 0;
+    const uint32_t parity = (ST == 2) ? (uint32_t)((it >> 1) & 1) : (uint32_t)(it & 1);
+    const int next = tile + gridDim.x;
+    if (ST == 2 && tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+
+    const TileDesc td = v.tiles[tile];
+    const int nd = td.ndials, ne = td.nevents;
+    for (int i = tid; i < nd; i += NT) {
+      const uint64_t h = v.hdr[td.dial0 + i];
+      shdr[hdr_slot(h)] = h;
+    }
+    for (int e = tid; e < ne; e += NT) {
+      sev[e] = v.evinfo[td.event0 + e];
+      sw0[e] = ((const T*)v.w0)[td.event0 + e];
+    }
+    if (tid == 0) sev[ne] = make_evinfo(nd, 0);
+    if (tid < kMaxLocalBins) s_present[tid] = 0;
+    const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(v.status, kStatusCopyTimeout);
+        if (ST == 2 && next < v.n_tiles)
+          mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      }
+      return;
+    }
+    for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
+    const T* pl = (const T*)(st ? stage1 : stage0);
+
+    // Each warp takes a contiguous run of events holding ~nd/NW dials: the
+    // first event whose first slot reaches warp*nd/NW (a fixed, deterministic
+    // split, so the FP64 summation order does not depend on scheduling).
+    auto first_event_at = [&](int target) {
+      int lo = 0, hi = ne;  // sev[ne] holds nd
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ev_slot(sev[mid]) < target) lo = mid + 1;
+        else hi = mid;
+      }
+      return lo;
+    };
+    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * nd) / NW);
+    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * nd) / NW);
+    const int sub = lane / KC, kl = lane % KC;
+
+    for (int kb = 0; kb < K; kb += KP) {
+      const int k0 = kb + kl;  // this lane's points: k0 + j*KC
+#pragma unroll
+      for (int lb = 0; lb < kMaxLocalBins; ++lb)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) wpart[((lb * NW + warp) * KR + j) * 32 + lane] = make_double2(0.0, 0.0);
+      int cur = -1;
+      double s[KR], s2[KR];
+#pragma unroll
+      for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
+      for (int base = e_lo; base < e_hi; base += EPW) {
+        const int e = base + sub;
+        if (e < e_hi) {
+          const uint16_t ei = sev[e];
+          const int s0 = ev_slot(ei), s1 = ev_slot(sev[e + 1]);
+          T w[KR];
+#pragma unroll
+          for (int j = 0; j < KR; ++j) w[j] = T(1);
+          for (int sl = s0; sl < s1; ++sl) {
+            T val[KR];
+            dial_values<T, KR>(v, shdr[sl], pl, k0, KC, val);
+#pragma unroll
+            for (int j = 0; j < KR; ++j) w[j] *= val[j];
+          }
+          const T w0 = sw0[e];
+          const int lb = ev_lbin(ei);
+          if (lb != cur) {
+            if (cur >= 0) {
+#pragma unroll
+              for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
+            }
+            cur = lb;
+#pragma unroll
+            for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < KR; ++j) {
+            T wj = w[j];
+            if (v.has_cap && wj > (T)v.cap) wj = (T)v.cap;
+            wj = w0 * wj;
+            const double wd = (double)wj;
+            s[j] += wd;
+            s2[j] += wd * wd;
+          }
+        }
+      }
+      if (cur >= 0) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j) wpart[((cur * NW + warp) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
+      }
+      __syncthreads();
+      for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
+        const int lb = t / KP, r = t % KP;
+        const int j = r / KC, kk = r % KC;
+        const int kg = kb + kk + j * KC;
+        if (kg < K && lb < (int)td.nbins && s_present[lb]) {
+          double a = 0.0, a2 = 0.0;
+          for (int w = 0; w < NW; ++w) {
+#pragma unroll
+            for (int sb = 0; sb < EPW; ++sb) {
+              const double2 p = wpart[((lb * NW + w) * KR + j) * 32 + sb * KC + kk];
+              a += p.x;
+              a2 += p.y;
+            }
+          }
+          const int slot = (lb == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + lb];
+          v.partials[(size_t)slot * v.kpad + kg] = make_double2(a, a2);
+        }
+      }
+      __syncthreads();
+    }
+    if (ST == 1 && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
+  }
+}
+
+template <typename T, int KC, int KR, int NT, int ST>
+void launch_b(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
+  k_batched<T, KC, KR, NT, ST><<<grid, NT, smem, s>>>(v, K);
+}
+
+#define GW_SHAPE(KC, KR, NT, ST)                                                               \
+  {0, KC, KR, NT, ST, {(const void*)k_batched<double, KC, KR, NT, ST>,                        \
+                       (const void*)k_batched<float, KC, KR, NT, ST>},                         \
+   {launch_b<double, KC, KR, NT, ST>, launch_b<float, KC, KR, NT, ST>}}
+
+const ShapeEntry kLaneShapes[] = {
+    GW_SHAPE(8, 1, 256, 2),  GW_SHAPE(16, 1, 256, 2), GW_SHAPE(32, 1, 256, 2), GW_SHAPE(32, 1, 256, 1),
+    GW_SHAPE(32, 2, 256, 1), GW_SHAPE(32, 2, 256, 2), GW_SHAPE(32, 2, 128, 1), GW_SHAPE(32, 4, 128, 1),
+    GW_SHAPE(16, 2, 256, 1), GW_SHAPE(32, 4, 256, 1),
+};
+#undef GW_SHAPE
+
+}  // namespace
+
+int lane_shapes(const ShapeEntry** out) {
+  *out = kLaneShapes;
+  return (int)(sizeof(kLaneShapes) / sizeof(kLaneShapes[0]));
+}
+
+}  // namespace gw

@@ -147,10 +147,11 @@ class Engine:
     def autotune(self, K): self._chk(self.lib.gw_autotune(self._e, K))
 
     def shape(self):
-        """(points per warp pass, threads per block, payload stages) of the batched kernel."""
-        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
-        self._chk(self.lib.gw_get_shape(self._e, C.byref(a), C.byref(b), C.byref(c)))
-        return a.value, b.value, c.value
+        """(kernel family, points per pass, threads per block, payload stages) of the batched kernel;
+        family 0 = k_batched (lanes over points), 1 = k_multi (threads over dials)."""
+        k, a, b, c = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        self._chk(self.lib.gw_get_shape(self._e, C.byref(k), C.byref(a), C.byref(b), C.byref(c)))
+        return k.value, a.value, b.value, c.value
 
     def set_event_weight_copy(self, on=True): self._chk(self.lib.gw_set_event_weight_copy(self._e, int(on)))
 
