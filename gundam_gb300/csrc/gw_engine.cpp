@@ -630,10 +630,13 @@ void write_prepared(const DialRec& r, const double* d, int n, float* out) {
   }
 }
 
-// Stored elements of a dial in the engine precision.
+// Stored elements of a dial in the engine precision.  Non-empty payloads are
+// padded to an odd element count: threads that read consecutive same-type
+// dials then hit distinct shared-memory banks.
 int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool fp32) {
-  if (fp32 && (r.type == kMonotonic || r.type == kCompact)) return 2 + 2 * n;
-  return raw;
+  int32_t el = (fp32 && (r.type == kMonotonic || r.type == kCompact)) ? 2 + 2 * n : raw;
+  if (el > 0 && (el & 1) == 0) ++el;
+  return el;
 }
 
 struct TilePlan {
@@ -1267,6 +1270,25 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
   e->graphs.clear();
   return check_status(e);
+}
+
+extern "C" int gw_set_shape(gw_engine* e, int32_t kind, int32_t kc, int32_t threads, int32_t stages) {
+  if (!e) return GW_ERR_ARG;
+  if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
+  GW_CUDA(e, cudaSetDevice(e->device));
+  for (int i = 0; i < batched_shape_count(); ++i) {
+    const BatchedShape b = batched_shape(i);
+    const int per_pass = b.kind == 0 ? b.kc * b.kr : b.kc;
+    if (b.kind != kind || per_pass != kc || b.threads != threads || b.stages != stages) continue;
+    const int bps = batched_blocks_per_sm(e->view, b);
+    if (bps < 1) return fail(e, GW_ERR_ARG, "shape does not fit on an SM");
+    e->shape = b;
+    e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
+    for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
+    e->graphs.clear();
+    return GW_OK;
+  }
+  return fail(e, GW_ERR_ARG, "no compiled shape (%d, %d, %d, %d)", kind, kc, threads, stages);
 }
 
 extern "C" int gw_get_shape(const gw_engine* e, int32_t* kind, int32_t* kc, int32_t* threads, int32_t* stages) {

@@ -9,8 +9,8 @@ namespace {
 // K > 1, dial-parallel: the plain kernel's mapping (threads over the tile's
 // type-ordered dials, so a warp runs one dial type at a time) with each thread
 // evaluating its dial for KR consecutive points, a chunk of KCH = KR*KS points
-// per pass over the tile.  Per chunk: dial values -> dval[slot][KCH]; ordered
-// per-event products -> wsh[event][KCH] (FP64); one warp per (bin, point)
+// per pass over the tile.  Per chunk: dial values -> dval[KCH][slot]; ordered
+// per-event products -> wsh[KCH][event] (FP64); one warp per (bin, point)
 // reduces the tile's events of that bin.  The payload stays in shared memory
 // for all K points.
 // ---------------------------------------------------------------------------
@@ -22,8 +22,8 @@ __global__ void __launch_bounds__(256) k_multi(const DevView v, int K) {
   unsigned char* stage0 = smem;
   unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
   uint64_t* shdr = (uint64_t*)(smem + ST * TB);        // [1024], tile order
-  double* wsh = (double*)(shdr + 1024);                 // [256][KCH]
-  T* dval = (T*)(wsh + kMaxTileEvents * KCH);           // [1024][KCH]
+  double* wsh = (double*)(shdr + 1024);                 // [KCH][256]
+  T* dval = (T*)(wsh + kMaxTileEvents * KCH);           // [KCH][1024]
   T* sw0 = dval + 1024 * KCH;                           // [256]
   uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);   // [257]
   __shared__ uint64_t bar[2];
@@ -81,20 +81,21 @@ __global__ void __launch_bounds__(256) k_multi(const DevView v, int K) {
         const uint64_t h = shdr[i];
         T val[KR];
         dial_values<T, KR>(v, h, pl, kb + ks * KR, 1, val);
-        T* dst = dval + hdr_slot(h) * KCH + ks * KR;
+        T* dst = dval + (ks * KR) * 1024 + hdr_slot(h);
 #pragma unroll
-        for (int j = 0; j < KR; ++j) dst[j] = val[j];
+        for (int j = 0; j < KR; ++j) dst[j * 1024] = val[j];
       }
       __syncthreads();
       // ordered per-event products (EventDialCache.cpp:156-171)
       for (int t = tid; t < ne * KCH; t += NT) {
-        const int e = t / KCH, j = t - e * KCH;
+        const int j = t / ne, e = t - j * ne;
         const int s0 = ev_slot(sev[e]), s1 = ev_slot(sev[e + 1]);
+        const T* dv = dval + j * 1024;
         T w = T(1);
-        for (int s = s0; s < s1; ++s) w *= dval[s * KCH + j];
+        for (int s = s0; s < s1; ++s) w *= dv[s];
         if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
         w = sw0[e] * w;
-        wsh[e * KCH + j] = (double)w;
+        wsh[j * kMaxTileEvents + e] = (double)w;
       }
       __syncthreads();
       // one warp per (local bin, point): fixed-order FP64 sums of w and w^2
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(256) k_multi(const DevView v, int K) {
         if (b1 > b0 && kb + j < K) {
           double s = 0.0, s2 = 0.0;
           for (int e = b0 + lane; e < b1; e += 32) {
-            const double w = wsh[e * KCH + j];
+            const double w = wsh[j * kMaxTileEvents + e];
             s += w;
             s2 += w * w;
           }

@@ -153,6 +153,9 @@ class Engine:
         self._chk(self.lib.gw_get_shape(self._e, C.byref(k), C.byref(a), C.byref(b), C.byref(c)))
         return k.value, a.value, b.value, c.value
 
+    def set_shape(self, kind, points_per_pass, threads, stages):
+        self._chk(self.lib.gw_set_shape(self._e, kind, points_per_pass, threads, stages))
+
     def set_event_weight_copy(self, on=True): self._chk(self.lib.gw_set_event_weight_copy(self._e, int(on)))
 
     def event_weights(self) -> np.ndarray:

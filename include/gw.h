@@ -221,6 +221,10 @@ int gw_use_graph(gw_engine* e, int32_t on);
  * (points per warp pass x threads per block x payload stages). */
 int gw_autotune(gw_engine* e, int32_t K);
 
+/* Selects a batched shape by hand (the values gw_get_shape reports);
+ * GW_ERR_ARG when no such compiled shape exists or it does not fit. */
+int gw_set_shape(gw_engine* e, int32_t kind, int32_t points_per_pass, int32_t threads, int32_t stages);
+
 /* Copies the batched shape in use out: kernel family (0 = lanes over points,
  * 1 = threads over dials), parameter points per pass, threads per block,
  * payload stages. */
