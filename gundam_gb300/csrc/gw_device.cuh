@@ -181,5 +181,43 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
   }
 }
 
+// Per-bin likelihoods.
+__device__ __forceinline__ double llh_poisson(double data, double pred) {
+  // PoissonLogLikelihood.h:19-53
+  if (pred <= 0.0) return HUGE_VAL;
+  if (data <= 0.0) return 2.0 * pred;
+  return 2.0 * (pred - data + data * log(data / pred));
+}
+
+__device__ __forceinline__ double llh_bb_oa2021(double data, double pred, double mcuncert) {
+  // BarlowBeestonBanff2022.h:150-294 with its defaults (expectedValueMinimum
+  // = -1, fractionalErrorLimit = 1e150, usePoissonLikelihood = false).
+  if (pred <= -1.0) {
+    if (pred <= 0.0 && data > 0.0) return HUGE_VAL;
+    return 0.0;
+  }
+  double newmc = pred;
+  double penalty = 0.0;
+  if (mcuncert > 0.0) {
+    const double fractional = fmin(sqrt(mcuncert) / pred, 1.0e150);
+    const double temp = pred * fractional * fractional - 1;
+    const double temp2 = temp * temp + 4 * data * fractional * fractional;
+    if (temp2 < 0) return HUGE_VAL;
+    const double beta = (-1 * temp + sqrt(temp2)) / 2.;
+    newmc = fmax(pred * beta, DBL_MIN);
+    penalty = (beta - 1) * (beta - 1) / (2 * fractional * fractional);
+  }
+  double stat;
+  if (data <= DBL_EPSILON) {
+    stat = newmc;
+  } else if (newmc > DBL_MIN) {
+    stat = newmc - data + data * (log(data) - log(newmc));
+  } else {
+    const double mc = DBL_MIN;
+    stat = mc - data + data * (log(data) - log(mc));
+  }
+  return 2.0 * stat + 2.0 * penalty;
+}
+
 }  // namespace
 }  // namespace gw

@@ -1366,3 +1366,6 @@ extern "C" int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weight
   e->kernel_launches = 0;
   return GW_OK;
 }
+
+// Error text of calls that have no engine (read with gw_last_error(NULL, ...)).
+void gw_internal_set_error(const char* msg) { g_create_error = msg ? msg : ""; }

@@ -249,6 +249,23 @@ int gw_set_profiling(gw_engine* e, int32_t on);
  * kernel_launches counts every engine kernel launched.  Resets the sums. */
 int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weights_launches, int64_t* kernel_launches);
 
+/* Likelihood from bin sums the caller holds on the device, with no device
+ * allocation.  No counterpart in the reference.  For callers that cannot call
+ * cudaMalloc: code running inside a framework that owns the GPU's memory (a
+ * caching allocator or a fitter's pool), or per-evaluation callbacks that must
+ * not let cudaMalloc/cudaFree synchronise the device.
+ *   d_sums, d_sums2 [K * n_bins]  sum of w and of w^2 per bin (device)
+ *   d_data          [n_bins]      observed counts (device)
+ *   d_llh           [K]           output: the summed per-bin likelihood (device)
+ * Same per-bin terms and reduction order as gw_eval's llh_stat.  Scratch is a
+ * fixed array inside the library (65536 block partials + 4096 counters, about
+ * 528 KiB per GPU, held until exit): K <= 4096 and K * ceil(n_bins/256) <=
+ * 65536, else GW_ERR_LIMIT.  All calls share that array: calls that overlap on
+ * the GPU race.  The first call on a device looks up the array's address; make
+ * it before any stream capture.  Asynchronous on `stream`. */
+int gw_llh_noalloc(const double* d_sums, const double* d_sums2, const double* d_data, int32_t n_bins, int32_t K,
+                   int32_t llh_type, double* d_llh, void* stream);
+
 /* Layout facts for measurement: tiles, dials, payload bytes, algorithmic
  * bytes read per evaluation pass. */
 typedef struct gw_layout_info {
