@@ -63,6 +63,22 @@ def dist_setup(args):
     return world, rank, local, dist
 
 
+def max_over_ranks(x: float, dist, device="cuda") -> float:
+    """Largest value over all ranks (the slowest rank's time)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all ranks processed divided by the (max-over-ranks) time."""
+    return world * units_per_rank / seconds
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -233,11 +249,8 @@ def run_gw(args, world, rank, local, dist):
     clocks.start()
     ms, kernel_ms, launches = time_device(eng, torch, d, K, args.steps, args.warmup, dist)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * K / (ms / 1e3)
+    ms = max_over_ranks(ms, dist)
+    value = whole_job_rate(K, world, ms / 1e3)
 
     # e2e through the public API with host buffers (params H2D, bins + LLH D2H each step)
     for _ in range(2):
@@ -248,11 +261,8 @@ def run_gw(args, world, rank, local, dist):
     for _ in range(args.steps):
         eng.eval(pts)
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * K / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": K * wl.n_params * 8,
+    e2e_s = max_over_ranks(e2e_s, dist)
+    e2e = {"value": whole_job_rate(K, world, e2e_s), "unit": "evals/s", "h2d_bytes_per_step": K * wl.n_params * 8,
            "d2h_bytes_per_step": K * wl.n_bins * 16 + K * 16, "ms_per_step": e2e_s * 1e3}
 
     peak, peak_kind = peaks()

@@ -158,6 +158,7 @@ GW_SIGNATURES: dict[str, list] = {
     "gw_get_layout": [_P, _P],
     "gw_set_profiling": [_P, _I32],
     "gw_llh_noalloc": [_P, _P, _P, _I32, _I32, _I32, _P, _P],
+    "gw_selftest_wait_timeout": [C.c_uint32, _P],
     "gw_read_profile": [_P, _P, _P, _P],
 }
 

@@ -15,6 +15,7 @@
 //               and reduce it, deterministically, to one value per point.
 // The reference needs ~1 + n_types + 2*(2 + log2 max bin occupancy) launches
 // for the same work (CacheWeights.cpp:153-183, CacheRecursiveSums.cpp:282-352).
+#include "gw.h"
 #include "gw_device.cuh"
 
 namespace gw {
@@ -399,3 +400,39 @@ cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2
 }
 
 }  // namespace gw
+
+// ---------------------------------------------------------------------------
+// Failure-path self-test: an mbarrier that expects bytes no copy will ever
+// deliver (nothing is in flight).  The bounded wait must give up after
+// limit_us and report it, leaving the context usable.
+// ---------------------------------------------------------------------------
+namespace gw {
+namespace {
+__global__ void k_selftest_wait(uint64_t limit_ns, uint32_t* status) {
+  __shared__ uint64_t bar;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  mbar_expect_tx(&bar, 16u);  // arrives, but 16 bytes stay pending forever
+  const bool ok = mbar_wait_bounded(&bar, 0u, limit_ns);
+  *status = ok ? 0u : kStatusCopyTimeout;
+}
+}  // namespace
+}  // namespace gw
+
+extern "C" int gw_selftest_wait_timeout(uint32_t limit_us, int32_t* timed_out) {
+  if (!timed_out || limit_us == 0 || limit_us > 1000000u) return GW_ERR_ARG;
+  uint32_t* d = nullptr;
+  if (cudaMalloc(&d, sizeof(uint32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    return GW_ERR_CUDA;
+  }
+  cudaMemset(d, 0xFF, sizeof(uint32_t));
+  gw::k_selftest_wait<<<1, 1>>>((uint64_t)limit_us * 1000ull, d);
+  uint32_t h = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return GW_ERR_CUDA;
+  *timed_out = (h == gw::kStatusCopyTimeout) ? 1 : 0;
+  return GW_OK;
+}

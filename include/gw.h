@@ -266,6 +266,11 @@ int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weights_launches,
 int gw_llh_noalloc(const double* d_sums, const double* d_sums2, const double* d_data, int32_t n_bins, int32_t K,
                    int32_t llh_type, double* d_llh, void* stream);
 
+/* Failure-path self-test (no reference counterpart): launches one block whose
+ * bounded wait on a bulk-copy barrier cannot complete, with limit_us (<= 1 s)
+ * as the limit.  timed_out = 1 when the wait gave up and reported it. */
+int gw_selftest_wait_timeout(uint32_t limit_us, int32_t* timed_out);
+
 /* Layout facts for measurement: tiles, dials, payload bytes, algorithmic
  * bytes read per evaluation pass. */
 typedef struct gw_layout_info {
