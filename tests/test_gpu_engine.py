@@ -62,7 +62,7 @@ def test_bounded_wait_gives_up_and_reports():
     assert t.value == 1
     # the context is still usable afterwards
     wl = Workload("mixed", seed=2)
-    eng = Engine.from_workload(wl, precision="fp64", k_max=1)
+    eng = Engine.from_workload(wl, precision="fp64", k_max=1, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
     s, s2, l, st = eng.eval(wl.nominal())
     assert np.isfinite(l[0])
     eng.close()
