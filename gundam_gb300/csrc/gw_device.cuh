@@ -137,14 +137,12 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       if (type == kMonotonic) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
-          else val[j] = eval_catmull<T, true>(d, n, x[j], trunc);
+          val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
         }
       } else if (type == kUniform) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<false>(d, n, x[j], trunc);
-          else val[j] = eval_uniform<T>(d, n, x[j], trunc);
+          val[j] = eval_prepared<T, false>(d, n, x[j], trunc);
         }
       } else if (type == kGeneral) {
 #pragma unroll
@@ -159,8 +157,7 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       } else if (type == kCompact) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) {
-          if constexpr (sizeof(T) == 4) val[j] = eval_prepared<true>(d, n, x[j], trunc);
-          else val[j] = eval_catmull<T, false>(d, n, x[j], trunc);
+          val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
         }
       } else if (type == kBicubic) {
         const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;

@@ -147,25 +147,25 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
   return (p1 + fx * m);
 }
 
-// FP32 layout of the Catmull-Rom and uniform splines.  The host stores each
+// Engine layout of the Catmull-Rom and uniform splines.  The host stores each
 // knot's value and its slope in index units (for Catmull-Rom splines the
 // slope after the Fritsch-Carlson limiter, for uniform splines dydx*step) and
 // 1/step instead of step: d = [low, 1/step, (y, s) x n].  Inside the knot
 // range this is exactly the Hermite cubic the reference evaluates; beyond the
 // ends the reference's clamped neighbour indices make the outer slope equal
 // the end difference (CalculateMonotonicSpline.h:66-103), restored here.
-template <bool catmull>
-__device__ __forceinline__ float eval_prepared(const float* __restrict__ d, int n, float x, bool trunc) {
-  float xx = (x - d[0]) * d[1];
-  if (trunc) xx = fminf(fmaxf(xx, 0.f), (float)(n - 1));
-  const int ix = catmull ? ((xx < 0.f) ? (int)(xx - 1.f) : (int)xx) : (int)xx;
+template <typename T, bool catmull>
+__device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, bool trunc) {
+  T xx = (x - d[0]) * d[1];
+  if (trunc) xx = (xx < T(0)) ? T(0) : ((xx > T(n - 1)) ? T(n - 1) : xx);
+  const int ix = catmull ? ((xx < T(0)) ? (int)(xx - T(1)) : (int)xx) : (int)xx;
   const int i = min(max(ix, 0), n - 2);
-  const float fx = xx - (float)i;
-  const float* k = d + 2 + 2 * i;
-  const float p1 = k[0];
-  float m1 = k[1];
-  const float p2 = k[2];
-  float m2 = k[3];
+  const T fx = xx - (T)i;
+  const T* k = d + 2 + 2 * i;
+  const T p1 = k[0];
+  T m1 = k[1];
+  const T p2 = k[2];
+  T m2 = k[3];
   if (catmull) {
     if (ix < 0) m2 = p2 - p1;
     if (ix > n - 2) m1 = p2 - p1;

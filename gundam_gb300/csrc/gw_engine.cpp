@@ -591,19 +591,20 @@ void write_payload(const DialRec& r, const double* d, T* out) {
   }
 }
 
-// FP32 layout of Catmull-Rom (monotonic, compact) and uniform splines:
+// Engine layout of Catmull-Rom (monotonic, compact) and uniform splines:
 // [low, 1/step, (y, s) x n] with s the knot slope in index units.  The
 // Catmull-Rom slope of knot k is the one CalculateMonotonicSpline.h:66-127
 // forms from its neighbours (with the Fritsch-Carlson limiter for monotonic
 // splines); the end knots get the end difference.  Computed here in FP64.
-void write_prepared(const DialRec& r, const double* d, int n, float* out) {
+template <typename T>
+void write_prepared(const DialRec& r, const double* d, int n, T* out) {
   const double low = d[0], step = d[1];
-  out[0] = (float)low;
-  out[1] = (float)(1.0 / step);
+  out[0] = (T)low;
+  out[1] = (T)(1.0 / step);
   if (r.type == kUniform) {
     for (int k = 0; k < n; ++k) {
-      out[2 + 2 * k] = (float)d[2 + 2 * k];
-      out[3 + 2 * k] = (float)(d[3 + 2 * k] * step);
+      out[2 + 2 * k] = (T)d[2 + 2 * k];
+      out[3 + 2 * k] = (T)(d[3 + 2 * k] * step);
     }
     return;
   }
@@ -625,8 +626,8 @@ void write_prepared(const DialRec& r, const double* d, int n, float* out) {
         if (s < -delta) s = -delta;
       }
     }
-    out[2 + 2 * k] = (float)y[k];
-    out[3 + 2 * k] = (float)s;
+    out[2 + 2 * k] = (T)y[k];
+    out[3 + 2 * k] = (T)s;
   }
 }
 
@@ -634,7 +635,8 @@ void write_prepared(const DialRec& r, const double* d, int n, float* out) {
 // padded to an odd element count: threads that read consecutive same-type
 // dials then hit distinct shared-memory banks.
 int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool fp32) {
-  int32_t el = (fp32 && (r.type == kMonotonic || r.type == kCompact)) ? 2 + 2 * n : raw;
+  (void)fp32;
+  int32_t el = (r.type == kMonotonic || r.type == kCompact) ? 2 + 2 * n : raw;
   if (el > 0 && (el & 1) == 0) ++el;
   return el;
 }
@@ -828,8 +830,8 @@ int build_and_upload(gw_engine* e) {
             const int p0 = r.type >= kTabulated ? (int)e->dial_data[(size_t)r.data_off] : r.p0;
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
             hdr[(size_t)(tp.dial0 + j)] = make_header(r.type, pn[(size_t)di], slot, off, p0, p1);
-            if (tsz == 4 && (r.type == kMonotonic || r.type == kCompact || r.type == kUniform))
-              write_prepared(r, e->dial_data.data() + r.data_off, pn[(size_t)di], (float*)(pl + off));
+            if (r.type == kMonotonic || r.type == kCompact || r.type == kUniform)
+              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off);
             else
               write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
             off += pel[(size_t)di];
