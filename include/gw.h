@@ -284,6 +284,31 @@ typedef struct gw_layout_info {
 } gw_layout_info;
 int gw_get_layout(const gw_engine* e, gw_layout_info* info);
 
+/* ---- learned surrogate: BF16 MLP on tensor cores (no reference counterpart) ----
+ * A fully connected network dims[0] -> dims[1] -> ... -> dims[n_layers] with
+ * SiLU between layers and a linear output, BF16 weights and activations with
+ * FP32 accumulation (tcgen05), FP32 master weights updated by Adam.  It maps a
+ * (standardised) parameter vector to predicted (standardised) log bin rates
+ * and serves as the first stage of the delayed-acceptance sampler.  Widths and
+ * batches must be multiples of 8. */
+typedef struct gwm_net gwm_net;
+int gwm_create(const int32_t* dims, int32_t n_layers, int32_t batch_max, int32_t device, gwm_net** net);
+int gwm_destroy(gwm_net* net);
+int gwm_last_error(const gwm_net* net, char* buf, size_t len);
+/* Layer l weights w [dims[l+1] x dims[l]] row-major and bias b [dims[l+1]] (host FP32). */
+int gwm_set_layer(gwm_net* net, int32_t layer, const float* w, const float* b);
+int gwm_get_layer(gwm_net* net, int32_t layer, float* w, float* b);
+/* y [B x dims[n]] = net(x [B x dims[0]]); FP32, host pointers or (device_ptrs != 0) device pointers. */
+int gwm_forward(gwm_net* net, const float* x, int32_t B, float* y, int32_t device_ptrs);
+/* One Adam step (beta 0.9 / 0.999) on the mean squared error of the batch; loss optional. */
+int gwm_train_step(gwm_net* net, const float* x, const float* t, int32_t B, float lr, int32_t device_ptrs,
+                   float* loss);
+/* Gradients of the mean squared error of a batch, without updating (host arrays per layer). */
+int gwm_gradients(gwm_net* net, const float* x, const float* t, int32_t B, float* const* grad_w,
+                  float* const* grad_b, float* loss);
+/* The tensor-core GEMM alone: C [M x N] = A [M x K] * B [N x K]^T, BF16 in (raw bits), FP32 out, host arrays. */
+int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, int32_t N, int32_t K, float* C);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,7 @@ def _declared(header: str, prefix: str):
 
 
 def test_every_engine_symbol_is_exported_and_bound():
-    names = _declared("gw.h", "gw_")
+    names = _declared("gw.h", "gw")
     assert len(names) >= 40
     lib = N.libgw()
     for n in names:
