@@ -38,7 +38,7 @@ def test_tcgen05_gemm_matches_fp64(M, N_, K):
     assert rc == 0
     ref = bf16_round(A) @ bf16_round(B).T
     err = np.abs(out - ref) / (np.sqrt(K) + np.abs(ref))
-    assert err.max() < 1e-5
+    assert err.max() < 3e-5  # FP32 accumulation over up to 4096 terms
 
 
 def _np_forward_backward(ws, bs, x, t):
