@@ -120,8 +120,8 @@ def test_training_lowers_loss_and_beats_affine_base():
     th = rng.standard_normal((8192, P))
     y = truth(th)
     s = Surrogate(P, B, hidden=(128, 128), batch_max=1024, seed=1)
-    hist = s.fit(th, y, epochs=12, lr=2e-3, batch=512)
-    assert hist[-1] < 0.3 * hist[0]
+    hist = s.fit(th, y, epochs=40, lr=2e-3, batch=512)
+    assert hist[-1] < 0.25 * hist[0]
     te = rng.standard_normal((1024, P))
     full = np.mean((s.log_rates(te) - truth(te)) ** 2)
     lin = np.mean((s.log_rates_linear(te) - truth(te)) ** 2)
