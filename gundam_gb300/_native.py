@@ -168,6 +168,8 @@ GW_SIGNATURES: dict[str, list] = {
     "gwm_train_step": [_P, _P, _P, _I32, C.c_float, _I32, _P],
     "gwm_gradients": [_P, _P, _P, _I32, _P, _P, _P],
     "gwm_gemm_test": [_P, _P, _I32, _I32, _I32, _P],
+    "gwm_set_head": [_P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "gwm_predict": [_P, _P, _I32, _I32, _P, _P],
     "gw_read_profile": [_P, _P, _P, _P],
 }
 

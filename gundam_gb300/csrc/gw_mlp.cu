@@ -323,6 +323,35 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
   }
 }
 
+// Standardised inputs: x = (theta - mean) / scale, FP32.
+__global__ void k_standardize(const double* __restrict__ theta, int rows, int cols, const float* __restrict__ mean,
+                              const float* __restrict__ scale, float* x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)rows * cols) return;
+  const int c = (int)(i % cols);
+  x[i] = (float)((theta[i] - (double)mean[c]) / (double)scale[c]);
+}
+
+// Head of the surrogate, one thread per (point, bin):
+//   log rate = b + sum_k x_k Wt[k][bin] + mu + sd * mlp  (FP32 affine base)
+//   sums = exp(log rate), sums2 = ratio * sums             (FP64 for the LLH)
+__global__ void k_head(const float* __restrict__ x, int din, const float* __restrict__ wt,
+                       const float* __restrict__ b0, const float* __restrict__ mu, const float* __restrict__ sd,
+                       const float* __restrict__ ratio, const float* __restrict__ mlp, int nb, double* sums,
+                       double* sums2, double* logr) {
+  const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y;
+  if (bin >= nb) return;
+  const float* xm = x + (size_t)m * din;
+  float acc = b0[bin];
+  for (int k = 0; k < din; ++k) acc = fmaf(xm[k], wt[(size_t)k * nb + bin], acc);
+  const double lr = (double)acc + (double)mu[bin] + (double)sd[bin] * (double)mlp[(size_t)m * nb + bin];
+  const double sv = exp(lr);
+  sums[(size_t)m * nb + bin] = sv;
+  sums2[(size_t)m * nb + bin] = (double)ratio[bin] * sv;
+  if (logr) logr[(size_t)m * nb + bin] = lr;
+}
+
 }  // namespace
 }  // namespace gwm
 
@@ -351,6 +380,12 @@ struct gwm_net {
   uint32_t* status = nullptr;
   int64_t step = 0;
   std::string err;
+  // surrogate head (gwm_set_head / gwm_predict)
+  bool has_head = false;
+  float *h_mean = nullptr, *h_scale = nullptr, *h_wt = nullptr, *h_b0 = nullptr, *h_mu = nullptr, *h_sd = nullptr,
+        *h_ratio = nullptr;
+  double *h_data = nullptr, *h_theta = nullptr, *h_sums = nullptr, *h_sums2 = nullptr, *h_llh = nullptr,
+         *h_logr = nullptr;
 };
 
 static thread_local std::string g_gwm_err;
@@ -657,4 +692,70 @@ extern "C" int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, in
   for (void* p : tmp.allocs) cudaFree(p);
   cudaStreamDestroy(tmp.stream);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Surrogate head: standardisation, affine base, output scaling, rate -> LLH.
+// ---------------------------------------------------------------------------
+extern "C" int gwm_set_head(gwm_net* n, const float* in_mean, const float* in_scale, const float* base_w,
+                            const float* base_b, const float* out_mu, const float* out_sd, const float* ratio,
+                            const double* data) {
+  if (!n || !in_mean || !in_scale || !base_w || !base_b || !out_mu || !out_sd || !ratio || !data) return GW_ERR_ARG;
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0], nb = n->dims[n->n_layers], Bm = n->batch_max;
+  if (!n->has_head) {
+    int rc = gwm_alloc(n, &n->h_mean, din) | gwm_alloc(n, &n->h_scale, din) |
+             gwm_alloc(n, &n->h_wt, (size_t)din * nb) | gwm_alloc(n, &n->h_b0, nb) | gwm_alloc(n, &n->h_mu, nb) |
+             gwm_alloc(n, &n->h_sd, nb) | gwm_alloc(n, &n->h_ratio, nb) | gwm_alloc(n, &n->h_data, nb) |
+             gwm_alloc(n, &n->h_theta, (size_t)Bm * din) | gwm_alloc(n, &n->h_sums, (size_t)Bm * nb) |
+             gwm_alloc(n, &n->h_sums2, (size_t)Bm * nb) | gwm_alloc(n, &n->h_llh, Bm) |
+             gwm_alloc(n, &n->h_logr, (size_t)Bm * nb);
+    if (rc) return rc;
+    n->has_head = true;
+  }
+  // base_w arrives as [nb x din]; stored transposed [din x nb] for the head kernel
+  std::vector<float> wt((size_t)din * nb);
+  for (int b = 0; b < nb; ++b)
+    for (int k = 0; k < din; ++k) wt[(size_t)k * nb + b] = base_w[(size_t)b * din + k];
+  GWM_CUDA(n, cudaMemcpy(n->h_mean, in_mean, sizeof(float) * din, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_scale, in_scale, sizeof(float) * din, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_wt, wt.data(), sizeof(float) * wt.size(), cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_b0, base_b, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_mu, out_mu, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_sd, out_sd, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_ratio, ratio, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_data, data, sizeof(double) * nb, cudaMemcpyHostToDevice));
+  return GW_OK;
+}
+
+// Surrogate statistical likelihood of B parameter points theta [B x din]
+// (host FP64): llh [B]; log_rates [B x nb] optional.  llh_type as gw_eval.
+extern "C" int gwm_predict(gwm_net* n, const double* theta, int32_t B, int32_t llh_type, double* llh,
+                           double* log_rates) {
+  if (!n || !theta || !llh || B < 1 || B > n->batch_max) return gwm_fail(n, GW_ERR_ARG, "gwm_predict: bad batch");
+  if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_predict: gwm_set_head has not been called");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0], nb = n->dims[n->n_layers], L = n->n_layers;
+  const int Bp = ((B + 7) / 8) * 8;  // GEMM rows in multiples of 8; the extra rows are zeros
+  if (Bp > n->batch_max) return gwm_fail(n, GW_ERR_ARG, "gwm_predict: batch above batch_max after padding");
+  if (Bp > B) GWM_CUDA(n, cudaMemsetAsync(n->h_theta, 0, sizeof(double) * (size_t)Bp * din, n->stream));
+  GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, theta, sizeof(double) * (size_t)B * din, cudaMemcpyHostToDevice, n->stream));
+  gwm::k_standardize<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->h_theta, Bp, din,
+                                                                                     n->h_mean, n->h_scale, n->xin);
+  gwm::k_to_bf16<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->xin, Bp, din, n->h[0],
+                                                                                    n->ht[0], Bp);
+  GWM_CUDA(n, cudaGetLastError());
+  int rc = forward(n, Bp);
+  if (rc) return rc;
+  gwm::k_head<<<dim3((nb + 255) / 256, B), 256, 0, n->stream>>>(n->xin, din, n->h_wt, n->h_b0, n->h_mu, n->h_sd,
+                                                                 n->h_ratio, n->z[L - 1], nb, n->h_sums, n->h_sums2,
+                                                                 log_rates ? n->h_logr : nullptr);
+  GWM_CUDA(n, cudaGetLastError());
+  rc = gw_llh_noalloc(n->h_sums, n->h_sums2, n->h_data, nb, B, llh_type, n->h_llh, n->stream);
+  if (rc) return gwm_fail(n, rc, "gwm_predict: likelihood reduction failed");
+  GWM_CUDA(n, cudaMemcpyAsync(llh, n->h_llh, sizeof(double) * B, cudaMemcpyDeviceToHost, n->stream));
+  if (log_rates)
+    GWM_CUDA(n, cudaMemcpyAsync(log_rates, n->h_logr, sizeof(double) * (size_t)B * nb, cudaMemcpyDeviceToHost,
+                                n->stream));
+  return check_status(n);
 }

@@ -1,0 +1,173 @@
+"""Random-walk Metropolis over batched chains, plain and delayed-acceptance.
+
+All log-densities here are GUNDAM's "-2 log L" convention: ``f(theta)`` =
+statistical likelihood + prior penalty, and a Metropolis step accepts with
+probability min(1, exp(-(f' - f) / 2)) -- the reference's SimpleMcmc uses
+-1/2 of its evalFit value as the log-likelihood (SimpleMcmc.cpp:1099-1116)
+with the TSimpleMCMC accept rule log U < delta log L (TSimpleMCMC.H:441-460).
+
+* ``plain``: every chain proposes theta' = theta + L z each step and every
+  proposal is evaluated by the exact engine (one batched evaluation of all
+  chains per step).
+* ``delayed``: stage 1 runs, per chain, ``n_sub`` Metropolis steps of the
+  same random walk on the surrogate density f_s.  That sub-chain is reversible
+  with respect to exp(-f_s/2), so using its end point phi as the proposal, the
+  exact Metropolis-Hastings ratio is (Christen & Fox 2005)
+      alpha = min(1, exp(-(f(phi) - f(theta))/2 + (f_s(phi) - f_s(theta))/2)),
+  which keeps exp(-f/2) exactly invariant however good the surrogate is.
+  Chains whose sub-chain did not move skip the exact evaluation.  When the
+  running mean of |(f(phi)-f(theta)) - (f_s(phi)-f_s(theta))| exceeds
+  ``max_error`` the sampler falls back to plain steps.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+
+def proposal_chol(prior_cov, scale=None):
+    P = prior_cov.shape[0]
+    s = (2.38 ** 2 / P) if scale is None else scale
+    return np.linalg.cholesky(s * prior_cov)
+
+
+def _mh_accept(rng, f_new, f_old):
+    u = rng.random(f_new.shape[0])
+    with np.errstate(over="ignore", invalid="ignore"):
+        return np.log(np.maximum(u, 1e-300)) < -(f_new - f_old) / 2.0
+
+
+def plain(f_exact, theta0, n_steps, L, seed=0, record=True):
+    rng = np.random.default_rng(seed)
+    th = np.array(theta0, dtype=np.float64)
+    C, P = th.shape
+    f = f_exact(th)
+    out = np.empty((n_steps, C, P)) if record else None
+    acc = 0
+    n_exact = C
+    t0 = time.perf_counter()
+    for s in range(n_steps):
+        prop = th + rng.standard_normal((C, P)) @ L.T
+        fp = f_exact(prop)
+        n_exact += C
+        a = _mh_accept(rng, fp, f)
+        th[a] = prop[a]
+        f[a] = fp[a]
+        acc += int(a.sum())
+        if record:
+            out[s] = th
+    dt = time.perf_counter() - t0
+    return {"chains": out, "accept": acc / (n_steps * C), "n_exact": n_exact, "seconds": dt}
+
+
+def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True):
+    rng = np.random.default_rng(seed)
+    th = np.array(theta0, dtype=np.float64)
+    C, P = th.shape
+    f = f_exact(th)
+    fs = f_sur(th)
+    out = np.empty((n_steps, C, P)) if record else None
+    stage1_moves = stage2_tries = stage2_acc = 0
+    n_exact = C
+    n_sur = C
+    err_hist = []
+    fell_back_at = None
+    t0 = time.perf_counter()
+    for s in range(n_steps):
+        if fell_back_at is not None:
+            prop = th + rng.standard_normal((C, P)) @ L.T
+            fp = f_exact(prop)
+            n_exact += C
+            a = _mh_accept(rng, fp, f)
+            th[a] = prop[a]
+            f[a] = fp[a]
+            fs[a] = np.nan
+            stage2_tries += C
+            stage2_acc += int(a.sum())
+            if record:
+                out[s] = th
+            continue
+        # stage 1: surrogate sub-chain of n_sub random-walk Metropolis steps
+        phi = th.copy()
+        fphi = fs.copy()
+        for _ in range(n_sub):
+            prop = phi + rng.standard_normal((C, P)) @ L.T
+            fprop = f_sur(prop)
+            n_sur += C
+            a = _mh_accept(rng, fprop, fphi)
+            phi[a] = prop[a]
+            fphi[a] = fprop[a]
+        moved = np.any(phi != th, axis=1)
+        stage1_moves += int(moved.sum())
+        if moved.any():
+            idx = np.nonzero(moved)[0]
+            fe = f_exact(phi[idx])
+            n_exact += idx.size
+            stage2_tries += idx.size
+            d_exact = fe - f[idx]
+            d_sur = fphi[idx] - fs[idx]
+            u = rng.random(idx.size)
+            with np.errstate(over="ignore", invalid="ignore"):
+                a = np.log(np.maximum(u, 1e-300)) < -(d_exact - d_sur) / 2.0
+            acc_idx = idx[a]
+            th[acc_idx] = phi[acc_idx]
+            f[acc_idx] = fe[a]
+            fs[acc_idx] = fphi[acc_idx]
+            stage2_acc += int(a.sum())
+            finite = np.isfinite(d_exact - d_sur)
+            err_hist.extend(np.abs(d_exact - d_sur)[finite].tolist())
+            recent = err_hist[-4 * C:]
+            if len(recent) >= C and np.mean(recent) > max_error:
+                fell_back_at = s
+        if record:
+            out[s] = th
+    dt = time.perf_counter() - t0
+    return {
+        "chains": out,
+        "stage1_move_rate": stage1_moves / (n_steps * C),
+        "stage2_accept": stage2_acc / max(stage2_tries, 1),
+        "accept": stage2_acc / (n_steps * C),
+        "n_exact": n_exact,
+        "n_surrogate": n_sur,
+        "seconds": dt,
+        "surrogate_error_mean": float(np.mean(err_hist)) if err_hist else None,
+        "fell_back_at_step": fell_back_at,
+    }
+
+
+def _autocorr(x):
+    n = x.shape[0]
+    x = x - x.mean(axis=0)
+    m = 1 << int(np.ceil(np.log2(2 * n)))
+    fx = np.fft.rfft(x, m, axis=0)
+    ac = np.fft.irfft(fx * np.conj(fx), m, axis=0)[:n]
+    v = ac[0]
+    v = np.where(v > 0, v, 1.0)
+    return ac / v
+
+
+def ess(chains, burn=0):
+    """Effective sample size per parameter, summed over chains, with Geyer's
+    initial positive (monotone) sequence estimator of the autocorrelation
+    time.  chains: [steps x chains x params]."""
+    x = chains[burn:]
+    n, C, P = x.shape
+    total = np.zeros(P)
+    for c in range(C):
+        rho = _autocorr(x[:, c, :])  # [n x P]
+        tau = np.ones(P)
+        for p in range(P):
+            r = rho[:, p]
+            g_prev = np.inf
+            s = 0.0
+            for m in range(0, (n - 1) // 2):
+                g = r[2 * m] + r[2 * m + 1]
+                if g <= 0:
+                    break
+                g = min(g, g_prev)
+                s += g
+                g_prev = g
+            tau[p] = max(1.0, -1.0 + 2.0 * s)
+        total += n / tau
+    return total

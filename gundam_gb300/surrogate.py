@@ -126,13 +126,16 @@ def cosine_lr(step, total, lr0, lr_min=0.0):
 
 def training_data(engine, wl, n, seed=0, inflate=1.5, k=64):
     """n parameter draws from the prior inflated by `inflate`, reweighted by
-    the exact engine: returns (theta [n x P], log sum of weights [n x B])."""
+    the exact engine: returns (theta [n x P], log sum of weights [n x B],
+    per-bin mean of sum(w^2)/sum(w))."""
     thetas = wl.draw_points(n, seed, inflate=inflate)
     logs = np.empty((n, wl.n_bins))
+    ratio = np.zeros(wl.n_bins)
     for s in range(0, n, k):
-        sums, _, _, _ = engine.eval(thetas[s:s + k])
+        sums, sums2, _, _ = engine.eval(thetas[s:s + k])
         logs[s:s + k] = np.log(np.maximum(sums, 1e-300))
-    return thetas, logs
+        ratio += (sums2 / np.maximum(sums, 1e-300)).sum(axis=0)
+    return thetas, logs, ratio / n
 
 
 class Surrogate:
@@ -182,6 +185,28 @@ class Surrogate:
         z = self._z(theta)
         base = np.hstack([np.ones((z.shape[0], 1)), z]) @ self.A
         return base + self.r_mu + self.r_sd * self.mlp.forward(z.astype(np.float32)).astype(np.float64)
+
+    def attach(self, data, ratio, llh_type):
+        """Moves the head (standardisation, affine base, output scaling, the
+        sum(w^2)/sum(w) ratio and the data) onto the GPU for ``stat_llh``."""
+        f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+        self.llh_type = int(llh_type)
+        _chk(N.libgw().gwm_set_head(self.mlp._n, _p(f32(self.mu)), _p(f32(self.sd)), _p(f32(self.A[1:].T)),
+                                    _p(f32(self.A[0])), _p(f32(self.r_mu)), _p(f32(self.r_sd)), _p(f32(ratio)),
+                                    _p(np.ascontiguousarray(data, dtype=np.float64))), self.mlp._n)
+
+    def stat_llh(self, theta):
+        """Surrogate statistical likelihood (-2 log L) of each parameter point, on the GPU."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        out = np.empty(th.shape[0])
+        bm = self.mlp.batch_max
+        for s in range(0, th.shape[0], bm):
+            part = np.ascontiguousarray(th[s:s + bm])
+            o = np.empty(part.shape[0])
+            _chk(N.libgw().gwm_predict(self.mlp._n, _p(part), part.shape[0], self.llh_type, _p(o), None),
+                 self.mlp._n)
+            out[s:s + part.shape[0]] = o
+        return out
 
     def log_rates_linear(self, theta):
         z = self._z(theta)

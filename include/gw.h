@@ -306,6 +306,16 @@ int gwm_train_step(gwm_net* net, const float* x, const float* t, int32_t B, floa
 /* Gradients of the mean squared error of a batch, without updating (host arrays per layer). */
 int gwm_gradients(gwm_net* net, const float* x, const float* t, int32_t B, float* const* grad_w,
                   float* const* grad_b, float* loss);
+/* Surrogate head: inputs are standardised as (theta - in_mean) / in_scale
+ * [dims[0]]; predicted log rate = base_b + base_w x + out_mu + out_sd * net(x)
+ * (base_w [dims[n] x dims[0]], FP32); Sum w^2 is modelled as ratio * rate; data
+ * [dims[n]] are the observed counts. */
+int gwm_set_head(gwm_net* net, const float* in_mean, const float* in_scale, const float* base_w,
+                 const float* base_b, const float* out_mu, const float* out_sd, const float* ratio,
+                 const double* data);
+/* Surrogate statistical likelihood (GW_LLH_*) of B points theta [B x dims[0]]
+ * (host FP64) -> llh [B] (host); log_rates [B x dims[n]] optional. */
+int gwm_predict(gwm_net* net, const double* theta, int32_t B, int32_t llh_type, double* llh, double* log_rates);
 /* The tensor-core GEMM alone: C [M x N] = A [M x K] * B [N x K]^T, BF16 in (raw bits), FP32 out, host arrays. */
 int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, int32_t N, int32_t K, float* C);
 

@@ -1,0 +1,76 @@
+"""Samplers on an analytic Gaussian target (CPU): plain and delayed
+acceptance recover the posterior, and delayed acceptance with an imperfect
+surrogate stays exact (the surrogate only changes efficiency)."""
+import numpy as np
+
+from gundam_gb300 import mcmc
+
+
+def _target(P=6, seed=0):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((P, P))
+    cov = A @ A.T / P + 0.5 * np.eye(P)
+    mean = rng.standard_normal(P)
+    icov = np.linalg.inv(cov)
+
+    def f(th):
+        d = th - mean
+        return np.einsum("ij,jk,ik->i", d, icov, d)
+    return mean, cov, icov, f
+
+
+def test_plain_recovers_gaussian():
+    mean, cov, icov, f = _target()
+    L = mcmc.proposal_chol(cov)
+    r = mcmc.plain(f, np.tile(mean, (32, 1)), 3000, L, seed=1)
+    x = r["chains"][500:].reshape(-1, mean.size)
+    assert np.allclose(x.mean(0), mean, atol=0.1)
+    assert np.allclose(x.std(0), np.sqrt(np.diag(cov)), rtol=0.1)
+    assert 0.15 < r["accept"] < 0.5
+
+
+def test_delayed_acceptance_is_exact_with_a_biased_surrogate():
+    mean, cov, icov, f = _target()
+    shift = 0.3 * np.sqrt(np.diag(cov))
+    icov_s = np.linalg.inv(1.3 * cov)
+
+    def f_sur(th):  # wrong mean and width
+        d = th - mean - shift
+        return np.einsum("ij,jk,ik->i", d, icov_s, d)
+    L = mcmc.proposal_chol(cov)
+    r = mcmc.delayed(f, f_sur, np.tile(mean, (32, 1)), 2500, L, n_sub=5, seed=2, max_error=1e9)
+    x = r["chains"][300:].reshape(-1, mean.size)
+    assert np.allclose(x.mean(0), mean, atol=0.12)
+    assert np.allclose(x.std(0), np.sqrt(np.diag(cov)), rtol=0.12)
+    assert r["fell_back_at_step"] is None
+
+
+def test_delayed_with_good_surrogate_gains_ess_per_exact_evaluation():
+    mean, cov, icov, f = _target()
+    L = mcmc.proposal_chol(cov)
+    th0 = np.tile(mean, (32, 1))
+    p = mcmc.plain(f, th0, 1500, L, seed=3)
+    d = mcmc.delayed(f, f, th0, 1500, L, n_sub=8, seed=4)
+    ess_p = mcmc.ess(p["chains"], burn=200).min() / p["n_exact"]
+    ess_d = mcmc.ess(d["chains"], burn=200).min() / d["n_exact"]
+    assert d["stage2_accept"] > 0.99  # exact surrogate: stage 2 always agrees
+    assert ess_d > 3 * ess_p
+
+
+def test_fallback_when_surrogate_error_grows():
+    mean, cov, icov, f = _target()
+    L = mcmc.proposal_chol(cov)
+
+    noise = np.random.default_rng(9)
+
+    def bad(th):  # disagrees with the target by ~10 units of -2 log L
+        return f(th) + noise.normal(0.0, 10.0, th.shape[0])
+    r = mcmc.delayed(f, bad, np.tile(mean, (16, 1)), 200, L, n_sub=4, seed=5, max_error=5.0)
+    assert r["fell_back_at_step"] is not None
+
+
+def test_ess_of_independent_draws_is_close_to_n():
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((4000, 4, 3))
+    e = mcmc.ess(x)
+    assert np.all(e > 0.8 * 16000) and np.all(e < 1.2 * 16000)
