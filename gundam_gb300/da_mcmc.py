@@ -37,7 +37,10 @@ def penalty(wl, icov, th):
 
 
 def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2, config="c2", log=print,
-        precision="fp32"):
+        precision="fp32", region="pilot", pilot_steps=200):
+    """region: where the training draws come from -- "prior" (the prior with
+    its covariance inflated x1.5) or "pilot" (a short plain-MCMC pilot run:
+    its sample mean with its sample covariance inflated x1.5)."""
     t_all = time.perf_counter()
     wl = Workload(config, n_events=events, seed=seed)
     llh_type = N.GW_LLH_BARLOW_BEESTON_OA2021 if config in ("c2", "c5") else N.GW_LLH_POISSON
@@ -51,8 +54,29 @@ def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2
             out[s:s + 64] = eng.eval(th[s:s + 64])[2]
         return out
 
+    L = mcmc.proposal_chol(wl.prior_cov)
+    th0 = wl.draw_points(chains, seed + 5, inflate=0.3)
+    # pilot / burn-in with the plain sampler (shared by both samplers below)
     t0 = time.perf_counter()
-    thetas, logs, ratio = training_data(eng, wl, train, seed=seed + 10, inflate=1.5)
+    pilot = mcmc.plain(f_exact, th0, pilot_steps, L, seed=seed + 6)
+    t_pilot = time.perf_counter() - t0
+    th0 = pilot["chains"][-1].copy()
+    pil = pilot["chains"][pilot_steps // 2:].reshape(-1, wl.n_params)
+    t0 = time.perf_counter()
+    if region == "prior":
+        thetas, logs, ratio = training_data(eng, wl, train, seed=seed + 10, inflate=1.5)
+    else:
+        mean = pil.mean(0)
+        cov = np.cov(pil.T) + 1e-12 * np.eye(wl.n_params)
+        rng = np.random.default_rng(seed + 10)
+        thetas = mean + 1.5 * rng.standard_normal((train, wl.n_params)) @ np.linalg.cholesky(cov).T
+        logs = np.empty((train, wl.n_bins))
+        ratio = np.zeros(wl.n_bins)
+        for s0 in range(0, train, 64):
+            sums, sums2, _, _ = eng.eval(thetas[s0:s0 + 64])
+            logs[s0:s0 + 64] = np.log(np.maximum(sums, 1e-300))
+            ratio += (sums2 / np.maximum(sums, 1e-300)).sum(axis=0)
+        ratio /= train
     t_data = time.perf_counter() - t0
     sur = Surrogate(wl.n_params, wl.n_bins, batch_max=4096, seed=seed)
     t0 = time.perf_counter()
@@ -63,19 +87,15 @@ def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2
     def f_sur(th):
         return sur.stat_llh(th) + penalty(wl, icov, th)
 
-    # surrogate error on held-out prior draws
-    hold = wl.draw_points(256, seed + 99)
-    ex = f_exact(hold)
-    sx = f_sur(hold)
-    d_ex = ex - ex.mean()
-    d_sx = sx - sx.mean()
-    sur_err = float(np.std(d_ex - d_sx))
+    # surrogate error (sd of the differences between points) on held-out
+    # prior draws and on held-out pilot-chain states
+    def err_sd(pts):
+        ex = f_exact(pts)
+        sx = f_sur(pts)
+        return float(np.std((ex - ex.mean()) - (sx - sx.mean())))
+    sur_err_prior = err_sd(wl.draw_points(256, seed + 99))
+    sur_err_post = err_sd(pil[np.random.default_rng(seed + 98).choice(pil.shape[0], 256, replace=False)])
 
-    L = mcmc.proposal_chol(wl.prior_cov)
-    th0 = wl.draw_points(chains, seed + 5, inflate=0.3)
-    # short common burn-in with the plain sampler
-    burn = mcmc.plain(f_exact, th0, max(20, steps // 10), L, seed=seed + 6, record=False)
-    del burn
     p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7)
     d = mcmc.delayed(f_exact, f_sur, th0, steps, L, n_sub=n_sub, seed=seed + 8)
     b = steps // 5
@@ -88,7 +108,9 @@ def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2
         "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
         "train_points": train, "epochs": epochs, "train_seconds": t_train, "data_seconds": t_data,
         "train_mse_first_last": [hist[0], hist[-1]],
-        "surrogate_llh_error_sd": sur_err,
+        "training_region": region, "pilot_steps": pilot_steps, "pilot_seconds": t_pilot,
+        "surrogate_llh_error_sd_prior_draws": sur_err_prior,
+        "surrogate_llh_error_sd_posterior": sur_err_post,
         "chains": chains, "steps": steps, "n_sub": n_sub,
         "plain": {"seconds": p["seconds"], "accept": p["accept"], "n_exact": p["n_exact"],
                   "ess_min": float(ess_p.min()), "ess_median": float(np.median(ess_p)),
@@ -121,8 +143,11 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--n-sub", type=int, default=10)
     ap.add_argument("--config", default="c2")
+    ap.add_argument("--region", default="pilot", choices=["pilot", "prior"])
+    ap.add_argument("--pilot-steps", type=int, default=200)
     a = ap.parse_args()
-    print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config)))
+    print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config,
+                         region=a.region, pilot_steps=a.pilot_steps)))
 
 
 if __name__ == "__main__":
