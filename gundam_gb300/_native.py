@@ -170,6 +170,15 @@ GW_SIGNATURES: dict[str, list] = {
     "gwm_gemm_test": [_P, _P, _I32, _I32, _I32, _P],
     "gwm_set_head": [_P, _P, _P, _P, _P, _P, _P, _P, _P],
     "gwm_predict": [_P, _P, _I32, _I32, _P, _P],
+    "gwm_set_head_additive": [_P, _P, _P, _I32, C.c_float, _P, _P, _P, _P, _P, _P, _P],
+    "gwm_set_chain": [_P, _P, _P, _P],
+    "gwm_substeps": [_P, _P, _P, _I32, _I32, _I32, C.c_uint64, _P, _P, _P],
+    "gwm_train_reserve": [_P, C.c_int64],
+    "gwm_train_size": [_P, _P],
+    "gwm_train_append": [_P, _P, _P, _I32, _I32],
+    "gwm_train_append_eval": [_P, _P, _P, _I32],
+    "gwm_train_read": [_P, _I64, _I32, _P, _P],
+    "gwm_train_epochs": [_P, _I32, _I32, C.c_float, C.c_float, C.c_uint64, _P],
     "gw_read_profile": [_P, _P, _P, _P],
 }
 

@@ -16,12 +16,15 @@
 // Forward: z = W x + b, h = silu(z); backward: dX = dY W (with the SiLU
 // derivative fused), dW = dY^T X; Adam on FP32 master weights refreshes the
 // BF16 weights and their transposes.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cfloat>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -137,48 +140,71 @@ struct Epilogue {
   int ld_t;             // leading dimension of out_bf16_t (>= M)
 };
 
-// Copies a rows x 64 BF16 tile (row-major source, K contiguous) into the
-// core-matrix layout: (r, k) -> (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2.
-__device__ __forceinline__ void load_tile(unsigned char* dst, const bf16* __restrict__ src, int rows, int row0,
-                                          int nrows_total, int K, int k0) {
-  const int chunks = rows * 8;  // 16-byte chunks
-  for (int c = threadIdx.x; c < chunks; c += kThreads) {
-    const int r = c >> 3, j = c & 7;
-    const int gr = row0 + r, gk = k0 + 8 * j;
-    uint4 val = make_uint4(0, 0, 0, 0);
-    if (gr < nrows_total) {
-      const bf16* p = src + (size_t)gr * K + gk;
-      if (gk + 8 <= K) {
-        val = *reinterpret_cast<const uint4*>(p);
-      } else if (gk < K) {
-        bf16 tmp[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) tmp[q] = (gk + q < K) ? p[q] : __float2bfloat16(0.f);
-        memcpy(&val, tmp, 16);
-      }
-    }
-    *reinterpret_cast<uint4*>(dst + (r >> 3) * 1024 + j * 128 + (r & 7) * 16) = val;
-  }
+// 2-D tiled TMA load of box {8 elements, R rows} at (k, row) into shared
+// memory, completing on an mbarrier (transaction bytes).
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int k, int row, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(k), "r"(row), "r"(smem_u32(bar))
+      : "memory");
 }
 
-template <int BN>
-__global__ void __launch_bounds__(kThreads) k_gemm(const bf16* __restrict__ A, const bf16* __restrict__ B, int M,
-                                                   int N, int K, Epilogue ep, uint32_t* status) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  constexpr int kATile = kBM * kBK * 2;  // 16 KB
-  constexpr int kBTile = BN * kBK * 2;
-  unsigned char* sa[2] = {smem, smem + kATile + kBTile};
-  unsigned char* sb[2] = {smem + kATile, smem + 2 * kATile + kBTile};
-  __shared__ uint64_t bar[2];
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Pipelined GEMM tile, C[128 x BN] = A[128 x K] * B[BN x K]^T.
+//   * thread 0 (warp 0) issues the TMA loads of each 64-wide K tile into one
+//     of S shared-memory stages (8 boxes of 8 K-elements per operand, so each
+//     stage holds core matrices (8 rows x 16 bytes) with LBO = rows * 16 bytes
+//     between K-neighbours and SBO = 128 bytes between row-neighbours);
+//     rows beyond M / N and columns beyond K arrive as zeros;
+//   * thread 32 (warp 1) waits for a stage, issues its four K = 16 MMAs and
+//     commits them to the stage's "empty" barrier, which lets the producer
+//     refill it; a final commit signals the epilogue;
+//   * all four warps read the accumulator from TMEM (warp w: rows 32w..32w+31)
+//     and store through a per-warp shared-memory transpose, so that row-major
+//     stores and gate loads are coalesced.
+// Every wait is bounded; on a timeout the tile records the failure in
+// *status, drains its own copies (bounded) and frees TMEM.
+template <int BN, int S>
+__global__ void __launch_bounds__(kThreads) k_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                   const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+                                                   Epilogue ep, uint32_t* status) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int kA = kBM * kBK * 2;  // 16 KB
+  constexpr int kB = BN * kBK * 2;
+  constexpr int kStage = kA + kB;
+  __shared__ __align__(8) uint64_t full[S], empty[S], done;
   __shared__ uint32_t tmem_base;
-  __shared__ int failed;
+  __shared__ volatile int failed;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
   if (warp == 0) tmem_alloc(&tmem_base, BN);
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     failed = 0;
   }
@@ -186,46 +212,62 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const bf16* __restrict__ A, c
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  constexpr uint32_t idesc = instr_desc(kBM, BN);
   const int nk = (K + kBK - 1) / kBK;
+  int produced = 0;
 
-  int issued = -1;  // last tile whose MMAs were issued
-  for (int kt = 0; kt < nk; ++kt) {
-    const int st = kt & 1;
-    if (kt >= 2) {
-      // the MMAs that read this stage two tiles ago must be done
-      const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)(((kt - 2) >> 1) & 1));
-      if (!ok) failed = 1;
-    }
-    __syncthreads();
-    if (failed) break;
-    issued = kt;
-    load_tile(sa[st], A, kBM, m0, M, K, kt * kBK);
-    load_tile(sb[st], B, BN, n0, N, K, kt * kBK);
-    fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(sa[st]), b0 = smem_u32(sb[st]);
-#pragma unroll
-      for (int s = 0; s < kBK / 16; ++s) {
-        const uint64_t ad = smem_desc(a0 + s * 256, 128, 1024);
-        const uint64_t bd = smem_desc(b0 + s * 256, 128, 1024);
-        mma_bf16(tmem, ad, bd, idesc, (kt > 0 || s > 0) ? 1u : 0u);
+  if (tid == 0) {
+    // producer
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % S;
+      if (kt >= S && !mbar_wait_bounded(&empty[st], (uint32_t)(((kt / S) - 1) & 1))) {
+        failed = 1;
+        break;
       }
-      mma_commit(&bar[st]);
+      if (failed) break;
+      unsigned char* a = smem + st * kStage;
+      unsigned char* b = a + kA;
+      mbar_arrive_expect(&full[st], (uint32_t)kStage);
+#pragma unroll
+      for (int j = 0; j < kBK / 8; ++j) {
+        tma_load_2d(a + j * (kBM * 16), &tmA, kt * kBK + 8 * j, m0, &full[st]);
+        tma_load_2d(b + j * (BN * 16), &tmB, kt * kBK + 8 * j, n0, &full[st]);
+      }
+      produced = kt + 1;
     }
+  } else if (tid == 32) {
+    // MMA issuer
+    constexpr uint32_t idesc = instr_desc(kBM, BN);
+    int kt = 0;
+    for (; kt < nk; ++kt) {
+      const int st = kt % S;
+      if (!mbar_wait_bounded(&full[st], (uint32_t)((kt / S) & 1))) {
+        failed = 1;
+        break;
+      }
+      if (failed) break;
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(smem + st * kStage), b0 = a0 + kA;
+#pragma unroll
+      for (int s16 = 0; s16 < kBK / 16; ++s16) {
+        const uint64_t ad = smem_desc(a0 + s16 * 2 * (kBM * 16), kBM * 16, 128);
+        const uint64_t bd = smem_desc(b0 + s16 * 2 * (BN * 16), BN * 16, 128);
+        mma_bf16(tmem, ad, bd, idesc, (kt > 0 || s16 > 0) ? 1u : 0u);
+      }
+      mma_commit(&empty[st]);
+    }
+    // covers every MMA issued above (or none)
+    mma_commit(&done);
   }
-  // wait for the last commit (it covers every earlier MMA of this thread)
-  if (!failed && issued >= 0) {
-    if (!mbar_wait_bounded(&bar[issued & 1], (uint32_t)((issued >> 1) & 1))) failed = 1;
-  }
+  __syncwarp();
+  const bool ok = mbar_wait_bounded(&done, 0);
+  if (!ok) failed = 1;
   __syncthreads();
   if (failed) {
     if (tid == 0) {
       atomicOr(status, 1u);
-      // wait once more (bounded) for MMAs still in flight before freeing TMEM
-      if (issued >= 0) mbar_wait_bounded(&bar[issued & 1], (uint32_t)((issued >> 1) & 1));
+      // drain the copies this tile issued (bounded) before the block exits
+      for (int kt = produced > S ? produced - S : 0; kt < produced; ++kt)
+        mbar_wait_bounded(&full[kt % S], (uint32_t)((kt / S) & 1));
     }
     tc_fence_before();
     __syncthreads();
@@ -234,28 +276,62 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const bf16* __restrict__ A, c
   }
   tc_fence_after();
 
-  // epilogue: warp w reads TMEM lanes 32w..32w+31 = tile rows
-  const int r = m0 + warp * 32 + lane;
+  // epilogue: the pipeline's shared memory is free now
+  float* tr = reinterpret_cast<float*>(smem) + warp * (32 * 33);
+  const int rbase = m0 + warp * 32;
+  const int r = rbase + lane;
   const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  for (int c0 = 0; c0 < BN; c0 += 8) {
-    float v[8];
-    tmem_ld8(lane_addr + (uint32_t)c0, v);
-    if (r >= M) continue;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int n = n0 + c0 + q;
-      if (n >= N) continue;
-      float z = v[q];
-      if (ep.bias) z += ep.bias[n];
-      if (ep.gate) {
-        const float g = ep.gate[(size_t)r * N + n];
-        const float sg = sigmoidf_(g);
-        z *= sg * (1.f + g * (1.f - sg));
+  for (int c0 = 0; c0 < BN; c0 += 32) {
+    if (n0 + c0 >= N) break;
+    float v[32];
+    tmem_ld32(lane_addr + (uint32_t)c0, v);
+    const int ncol = min(32, N - (n0 + c0));
+    if (ep.gate) {
+      // coalesced load of the gate tile [32 rows x 32 cols] -> transpose
+      __syncwarp();
+      for (int i = 0; i < 32; ++i) {
+        const int rr = rbase + i;
+        tr[i * 33 + lane] = (rr < M && lane < ncol) ? ep.gate[(size_t)rr * N + n0 + c0 + lane] : 0.f;
       }
-      if (ep.out_f32) ep.out_f32[(size_t)r * N + n] = z;
-      const float a = (ep.act == 1) ? z * sigmoidf_(z) : z;
-      if (ep.out_bf16) ep.out_bf16[(size_t)r * N + n] = __float2bfloat16(a);
-      if (ep.out_bf16_t) ep.out_bf16_t[(size_t)n * ep.ld_t + r] = __float2bfloat16(a);
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const float g = tr[lane * 33 + q];
+        const float sg = sigmoidf_(g);
+        v[q] *= sg * (1.f + g * (1.f - sg));
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q)
+      if (ep.bias && q < ncol) v[q] += ep.bias[n0 + c0 + q];
+    if (ep.out_f32) {
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 32; ++q) tr[lane * 33 + q] = v[q];
+      __syncwarp();
+      for (int i = 0; i < 32; ++i) {
+        const int rr = rbase + i;
+        if (rr < M && lane < ncol) ep.out_f32[(size_t)rr * N + n0 + c0 + lane] = tr[i * 33 + lane];
+      }
+    }
+    if (ep.out_bf16 || ep.out_bf16_t) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) v[q] = (ep.act == 1) ? v[q] * sigmoidf_(v[q]) : v[q];
+      if (ep.out_bf16_t && r < M) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q)
+          if (q < ncol) ep.out_bf16_t[(size_t)(n0 + c0 + q) * ep.ld_t + r] = __float2bfloat16(v[q]);
+      }
+      if (ep.out_bf16) {
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 32; ++q) tr[lane * 33 + q] = v[q];
+        __syncwarp();
+        for (int i = 0; i < 32; ++i) {
+          const int rr = rbase + i;
+          if (rr < M && lane < ncol) ep.out_bf16[(size_t)rr * N + n0 + c0 + lane] = __float2bfloat16(tr[i * 33 + lane]);
+        }
+      }
     }
   }
   tc_fence_before();
@@ -264,40 +340,86 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const bf16* __restrict__ A, c
 }
 
 // ---- small kernels ----
-__global__ void k_to_bf16(const float* __restrict__ x, int rows, int cols, bf16* y, bf16* yt, int ld_t) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)rows * cols) return;
-  const int r = (int)(i / cols), c = (int)(i % cols);
-  const bf16 v = __float2bfloat16(x[i]);
-  if (y) y[i] = v;
-  if (yt) yt[(size_t)c * ld_t + r] = v;
+// Rows of a row-major FP32 matrix to BF16, row-major and transposed.  Row r
+// of the output is row perm[r] of x (perm null: row r).  32 x 32 tiles go
+// through shared memory so both stores are coalesced; block (32, 8).
+__global__ void k_rows_to_bf16(const float* __restrict__ x, const int32_t* __restrict__ perm, int rows, int cols,
+                               bf16* y, bf16* yt, int ld_t) {
+  __shared__ bf16 tile[32][34];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, c = c0 + tx;
+    bf16 v = __float2bfloat16(0.f);
+    if (r < rows && c < cols) {
+      const size_t src = perm ? (size_t)perm[r] : (size_t)r;
+      v = __float2bfloat16(x[src * cols + c]);
+      if (y) y[(size_t)r * cols + c] = v;
+    }
+    tile[i][tx] = v;
+  }
+  if (!yt) return;
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int c = c0 + i, r = r0 + tx;
+    if (c < cols && r < rows) yt[(size_t)c * ld_t + r] = tile[tx][i];
+  }
 }
 
-// Mean squared error and its gradient: dy = 2 (y - t) / (rows * cols).
-__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, int rows, int cols, bf16* dy,
-                      bf16* dyt, int ld_t, float* loss) {
-  const int64_t n = (int64_t)rows * cols;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Mean squared error against target rows perm[r] of t (perm null: row r) and
+// its gradient dy = 2 (y - t) / (rows * cols), row-major and transposed
+// (tiled as k_rows_to_bf16).  loss += scale * sum e^2 / (rows * cols), one
+// atomic per block.
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, const int32_t* __restrict__ perm,
+                      int rows, int cols, bf16* dy, bf16* dyt, int ld_t, float* loss, float scale) {
+  __shared__ bf16 tile[32][34];
+  __shared__ float red[8];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const float inv = 1.f / ((float)rows * (float)cols);
   float e2 = 0.f;
-  if (i < n) {
-    const float e = y[i] - t[i];
-    e2 = e * e;
-    const bf16 g = __float2bfloat16(2.f * e / (float)n);
-    const int r = (int)(i / cols), c = (int)(i % cols);
-    dy[i] = g;
-    dyt[(size_t)c * ld_t + r] = g;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, c = c0 + tx;
+    bf16 g = __float2bfloat16(0.f);
+    if (r < rows && c < cols) {
+      const size_t tr = perm ? (size_t)perm[r] : (size_t)r;
+      const float e = y[(size_t)r * cols + c] - t[tr * cols + c];
+      e2 += e * e;
+      g = __float2bfloat16(2.f * e * inv);
+      dy[(size_t)r * cols + c] = g;
+    }
+    tile[i][tx] = g;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int c = c0 + i, r = r0 + tx;
+    if (c < cols && r < rows) dyt[(size_t)c * ld_t + r] = tile[tx][i];
   }
   for (int o = 16; o; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, e2 / (float)n);
+  if (tx == 0) red[ty] = e2;
+  __syncthreads();
+  if (ty == 0 && tx == 0) {
+    float b = 0.f;
+    for (int i = 0; i < 8; ++i) b += red[i];
+    atomicAdd(loss, b * inv * scale);
+  }
 }
 
-// Column sums of a row-major BF16 matrix (bias gradients), one thread per column.
+// Column sums of a row-major BF16 matrix (bias gradients): block (32, 16),
+// 32 columns per block, a fixed-order reduction over the 16 row strides.
 __global__ void k_colsum(const bf16* __restrict__ g, int rows, int cols, float* out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
+  __shared__ float part[16][33];
+  const int c = blockIdx.x * 32 + threadIdx.x;
   float s = 0.f;
-  for (int r = 0; r < rows; ++r) s += __bfloat162float(g[(size_t)r * cols + c]);
-  out[c] = s;
+  if (c < cols)
+    for (int r = threadIdx.y; r < rows; r += 16) s += __bfloat162float(g[(size_t)r * cols + c]);
+  part[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && c < cols) {
+    float t = 0.f;
+    for (int i = 0; i < 16; ++i) t += part[i][threadIdx.x];
+    out[c] = t;
+  }
 }
 
 // Adam on FP32 master weights; refreshes the BF16 copy and its transpose.
@@ -332,24 +454,197 @@ __global__ void k_standardize(const double* __restrict__ theta, int rows, int co
   x[i] = (float)((theta[i] - (double)mean[c]) / (double)scale[c]);
 }
 
-// Head of the surrogate, one thread per (point, bin):
-//   log rate = b + sum_k x_k Wt[k][bin] + mu + sd * mlp  (FP32 affine base)
-//   sums = exp(log rate), sums2 = ratio * sums             (FP64 for the LLH)
-__global__ void k_head(const float* __restrict__ x, int din, const float* __restrict__ wt,
-                       const float* __restrict__ b0, const float* __restrict__ mu, const float* __restrict__ sd,
-                       const float* __restrict__ ratio, const float* __restrict__ mlp, int nb, double* sums,
-                       double* sums2, double* logr) {
+// Surrogate head (device pointers).  The predicted log rate of a bin is
+//   base(x) + mu + sd * mlp(x)
+// with x the standardised parameters and base either affine (nodes == 0:
+// b0 + sum_k x_k tab[k][bin]) or additive piecewise-linear (nodes >= 2:
+// b0 + sum_k interp_k(x_k), interp_k linear between `nodes` equally spaced
+// values tab[k][0..nodes-1][bin] over x_k in [-lim, lim], constant outside).
+// Sum w^2 is modelled as exp(r_b + sum_k x_k r_w[k][bin]) * rate (r_w optional).
+struct Head {
+  int din, nb, nodes;
+  float lim;
+  const float* tab;
+  const float* b0;
+  const float* mu;
+  const float* sd;
+  const float* r_w;
+  const float* r_b;
+};
+
+__device__ __forceinline__ float head_base(const Head& h, const float* __restrict__ x, int bin) {
+  float acc = h.b0[bin];
+  if (h.nodes >= 2) {
+    const float inv_w = (float)(h.nodes - 1) / (2.f * h.lim);
+    for (int k = 0; k < h.din; ++k) {
+      const float xc = fminf(fmaxf(x[k], -h.lim), h.lim);
+      const float u = (xc + h.lim) * inv_w;
+      const int i = min((int)u, h.nodes - 2);
+      const float t = u - (float)i;
+      const float* T = h.tab + ((size_t)k * h.nodes + i) * h.nb + bin;
+      acc += fmaf(t, T[h.nb] - T[0], T[0]);
+    }
+  } else {
+    for (int k = 0; k < h.din; ++k) acc = fmaf(x[k], h.tab[(size_t)k * h.nb + bin], acc);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ double head_log_ratio(const Head& h, const float* __restrict__ x, int bin) {
+  float acc = h.r_b[bin];
+  if (h.r_w)
+    for (int k = 0; k < h.din; ++k) acc = fmaf(x[k], h.r_w[(size_t)k * h.nb + bin], acc);
+  return (double)acc;
+}
+
+// log(data / mc) for data, mc > 0: log1p((data - mc) / mc) near 1, where
+// log(data) - log(mc) would cancel in FP32, and the difference of logs away
+// from it, where the ratio itself can underflow or overflow.
+__device__ __forceinline__ float log_ratio_f(float data, float mc) {
+  const float r = (data - mc) / mc;
+  return fabsf(r) < 0.5f ? log1pf(r) : logf(data) - logf(mc);
+}
+
+// Per-bin likelihood term of the surrogate in FP32 (stage 1 only; the exact
+// engine keeps its FP64 path).  Same formulas as the engine's FP64 ones:
+// Poisson (PoissonLogLikelihood.h:19-53) and Barlow-Beeston OA2021
+// (BarlowBeestonBanff2022.h:150-294), with log(data / mc) from log_ratio_f.
+__device__ __forceinline__ float llh_term_f(int type, float data, float pred, float sumw2) {
+  if (type == GW_LLH_POISSON) {
+    if (pred <= 0.f) return INFINITY;
+    if (data <= 0.f) return 2.f * pred;
+    return 2.f * ((pred - data) + data * log_ratio_f(data, pred));
+  }
+  if (type != GW_LLH_BARLOW_BEESTON_OA2021) return 0.f;
+  if (pred <= -1.f) return (pred <= 0.f && data > 0.f) ? INFINITY : 0.f;
+  float newmc = pred, penalty = 0.f;
+  if (sumw2 > 0.f) {
+    const float f2 = sumw2 / (pred * pred);
+    const float temp = sumw2 / pred - 1.f;
+    const float temp2 = temp * temp + 4.f * data * f2;
+    if (temp2 < 0.f) return INFINITY;
+    const float beta = 0.5f * (sqrtf(temp2) - temp);
+    newmc = fmaxf(pred * beta, FLT_MIN);
+    penalty = (beta - 1.f) * (beta - 1.f) / (2.f * f2);
+  }
+  newmc = fmaxf(newmc, FLT_MIN);
+  float stat;
+  if (data <= FLT_EPSILON) stat = newmc;
+  else stat = (newmc - data) + data * log_ratio_f(data, newmc);
+  return 2.f * stat + 2.f * penalty;
+}
+
+// Head and likelihood terms, fused.  Block (32 bins, 8 point rows); thread
+// (x, y) of block (bx, by) handles bin 32 bx + x and the PPT points
+// by * 8 PPT + y + 8 j.  The block first stages, for each of its points and
+// parameters, the input x and (additive base) the table offset of the
+// interpolation interval and its weight in shared memory; the inner loop is
+// then two coalesced table loads and two FMAs per point and parameter, with
+// the table lines of a bin shared through L1 across the block's points.
+// Per point and block, the 32 bins' terms are summed by a fixed shuffle tree
+// into part[point][bx] (FP64); optional outputs: sums, sums2 (FP64), log rates.
+template <int PPT>
+__global__ void __launch_bounds__(256) k_head_llh(Head h, const float* __restrict__ x, const float* __restrict__ mlp,
+                                                  int C, const double* __restrict__ data, int llh_type,
+                                                  double* __restrict__ part, double* sums, double* sums2,
+                                                  double* logr) {
+  extern __shared__ unsigned char sh_raw[];
+  constexpr int NP = 8 * PPT;  // points per block
+  const int din = h.din;
+  float* s_z = reinterpret_cast<float*>(sh_raw);          // [NP][din]
+  float* s_t = s_z + NP * din;                            // [NP][din]
+  int* s_off = reinterpret_cast<int*>(s_t + NP * din);    // [NP][din]
+  const int mb = blockIdx.y * NP;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const bool additive = h.nodes >= 2;
+  const float inv_w = additive ? (float)(h.nodes - 1) / (2.f * h.lim) : 0.f;
+  for (int e = tid; e < NP * din; e += 256) {
+    const int ml = e / din, k = e - ml * din, m = mb + ml;
+    const float z = m < C ? x[(size_t)m * din + k] : 0.f;
+    s_z[e] = z;
+    if (additive) {
+      const float xc = fminf(fmaxf(z, -h.lim), h.lim);
+      const float u = (xc + h.lim) * inv_w;
+      const int i = min((int)u, h.nodes - 2);
+      s_t[e] = u - (float)i;
+      s_off[e] = (k * h.nodes + i) * h.nb;
+    } else {
+      s_t[e] = z;
+      s_off[e] = k * h.nb;
+    }
+  }
+  __syncthreads();
+  const int bin = blockIdx.x * 32 + threadIdx.x;
+  const bool bin_ok = bin < h.nb;
+  float acc[PPT], racc[PPT];
+#pragma unroll
+  for (int j = 0; j < PPT; ++j) {
+    acc[j] = bin_ok ? h.b0[bin] : 0.f;
+    racc[j] = bin_ok ? h.r_b[bin] : 0.f;
+  }
+  if (bin_ok) {
+    const float* tab = h.tab + bin;
+    const float* rw = h.r_w ? h.r_w + bin : nullptr;
+    const int nb = h.nb;
+    for (int k = 0; k < din; ++k) {
+      const float w = rw ? rw[(size_t)k * nb] : 0.f;
+#pragma unroll
+      for (int j = 0; j < PPT; ++j) {
+        const int e = (threadIdx.y + 8 * j) * din + k;
+        const int off = s_off[e];
+        const float t = s_t[e];
+        if (additive) {
+          const float lo = tab[off], hi = tab[off + nb];
+          acc[j] += fmaf(t, hi - lo, lo);
+        } else {
+          acc[j] = fmaf(t, tab[off], acc[j]);
+        }
+        racc[j] = fmaf(s_z[e], w, racc[j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PPT; ++j) {
+    const int m = mb + threadIdx.y + 8 * j;
+    float term = 0.f;
+    if (bin_ok && m < C) {
+      const size_t o = (size_t)m * h.nb + bin;
+      const float lr = acc[j] + h.mu[bin] + h.sd[bin] * mlp[o];
+      const float mu = expf(lr), s2 = expf(lr + racc[j]);
+      term = llh_term_f(llh_type, (float)data[bin], mu, s2);
+      if (sums) sums[o] = (double)mu;
+      if (sums2) sums2[o] = (double)s2;
+      if (logr) logr[o] = (double)lr;
+    }
+    double t = (double)term;
+    for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (threadIdx.x == 0 && m < C) part[(size_t)m * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// llh[m] = sum over blocks of part[m][*], one warp per point, fixed order.
+__global__ void k_llh_finish(const double* __restrict__ part, int nblk, int C, double* __restrict__ llh) {
+  const int m = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= C) return;
+  double s = 0.0;
+  for (int b = lane; b < nblk; b += 32) s += part[(size_t)m * nblk + b];
+  for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) llh[m] = s;
+}
+
+// Training target of a reweighted point, one thread per (point, bin):
+//   t = (log(sum of weights) - base(x) - mu) / sd
+// with the same FP32 base as k_head, so that k_head inverts it.
+__global__ void k_target(Head h, const float* __restrict__ x, const double* __restrict__ sums,
+                         float* __restrict__ t) {
   const int bin = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = blockIdx.y;
-  if (bin >= nb) return;
-  const float* xm = x + (size_t)m * din;
-  float acc = b0[bin];
-  for (int k = 0; k < din; ++k) acc = fmaf(xm[k], wt[(size_t)k * nb + bin], acc);
-  const double lr = (double)acc + (double)mu[bin] + (double)sd[bin] * (double)mlp[(size_t)m * nb + bin];
-  const double sv = exp(lr);
-  sums[(size_t)m * nb + bin] = sv;
-  sums2[(size_t)m * nb + bin] = (double)ratio[bin] * sv;
-  if (logr) logr[(size_t)m * nb + bin] = lr;
+  if (bin >= h.nb) return;
+  const float* xm = x + (size_t)m * h.din;
+  const double sv = sums[(size_t)m * h.nb + bin];
+  const double lr = log(sv > 1e-300 ? sv : 1e-300);
+  t[(size_t)m * h.nb + bin] = (float)((lr - (double)head_base(h, xm, bin) - (double)h.mu[bin]) / (double)h.sd[bin]);
 }
 
 }  // namespace
@@ -360,7 +655,11 @@ __global__ void k_head(const float* __restrict__ x, int din, const float* __rest
 // ---------------------------------------------------------------------------
 using gwm::bf16;
 
+struct gwm_chain_state;
+static void chain_free(gwm_chain_state* s);
+
 struct gwm_net {
+  gwm_chain_state* chain = nullptr;  // device state of the surrogate sub-chains (gwm_set_chain)
   int n_layers = 0;
   std::vector<int> dims;  // dims[0] = inputs, dims[L] = outputs
   int batch_max = 0;
@@ -382,10 +681,18 @@ struct gwm_net {
   std::string err;
   // surrogate head (gwm_set_head / gwm_predict)
   bool has_head = false;
-  float *h_mean = nullptr, *h_scale = nullptr, *h_wt = nullptr, *h_b0 = nullptr, *h_mu = nullptr, *h_sd = nullptr,
-        *h_ratio = nullptr;
+  int h_nodes = 0;
+  float h_lim = 0.f;
+  size_t h_tab_elems = 0;
+  bool h_has_rw = false;
+  float *h_mean = nullptr, *h_scale = nullptr, *h_tab = nullptr, *h_b0 = nullptr, *h_mu = nullptr, *h_sd = nullptr,
+        *h_rb = nullptr, *h_rw = nullptr;
   double *h_data = nullptr, *h_theta = nullptr, *h_sums = nullptr, *h_sums2 = nullptr, *h_llh = nullptr,
-         *h_logr = nullptr;
+         *h_logr = nullptr, *h_part = nullptr;
+  // training set on the device (gwm_train_reserve / gwm_train_append*):
+  // standardised inputs [train_max x dims[0]] and targets [train_max x dims[L]]
+  float *train_x = nullptr, *train_t = nullptr;
+  int64_t train_n = 0, train_max = 0;
 };
 
 static thread_local std::string g_gwm_err;
@@ -415,26 +722,70 @@ static int gwm_alloc(gwm_net* n, T** p, size_t count) {
   return GW_OK;
 }
 
-static size_t gemm_smem(int bn) { return 2 * (size_t)(gwm::kBM * gwm::kBK * 2 + bn * gwm::kBK * 2) + 1024; }
+constexpr int kStages = 4;
+static size_t gemm_smem(int bn) { return (size_t)kStages * (gwm::kBM * gwm::kBK * 2 + bn * gwm::kBK * 2) + 1024; }
 
-// C[M x N] = A[M x K] * B[N x K]^T with the given epilogue.
-static int gemm(gwm_net* n, const bf16* A, const bf16* B, int M, int N, int K, const gwm::Epilogue& ep) {
-  if (K % 8 != 0) return gwm_fail(n, GW_ERR_ARG, "GEMM K must be a multiple of 8");
-  const int bn = N >= 256 ? 256 : (N > 64 ? 128 : 64);
-  dim3 grid((N + bn - 1) / bn, (M + gwm::kBM - 1) / gwm::kBM);
-  const size_t smem = gemm_smem(bn);
-  if (bn == 256) {
-    GWM_CUDA(n, cudaFuncSetAttribute(gwm::k_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gwm::k_gemm<256><<<grid, gwm::kThreads, smem, n->stream>>>(A, B, M, N, K, ep, n->status);
-  } else if (bn == 128) {
-    GWM_CUDA(n, cudaFuncSetAttribute(gwm::k_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gwm::k_gemm<128><<<grid, gwm::kThreads, smem, n->stream>>>(A, B, M, N, K, ep, n->status);
-  } else {
-    GWM_CUDA(n, cudaFuncSetAttribute(gwm::k_gemm<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gwm::k_gemm<64><<<grid, gwm::kThreads, smem, n->stream>>>(A, B, M, N, K, ep, n->status);
-  }
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor map of a row-major BF16 matrix [rows x K] (K % 8 == 0, 16-byte
+// aligned rows) read in boxes of 8 K-elements x box_rows rows, zero fill.
+static int make_map(gwm_net* n, CUtensorMap* map, const bf16* p, int rows, int K, int box_rows) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return gwm_fail(n, GW_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  if (((uintptr_t)p & 15) != 0) return gwm_fail(n, GW_ERR_ARG, "GEMM operand not 16-byte aligned");
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)p, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return gwm_fail(n, GW_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return GW_OK;
+}
+
+template <int BN>
+static int launch_gemm(gwm_net* n, const bf16* A, const bf16* B, int M, int N, int K, const gwm::Epilogue& ep) {
+  CUtensorMap ma, mb;
+  int rc = make_map(n, &ma, A, M, K, gwm::kBM);
+  if (!rc) rc = make_map(n, &mb, B, N, K, BN);
+  if (rc) return rc;
+  const size_t smem = gemm_smem(BN);
+  static std::once_flag once;
+  std::call_once(once, [smem]() {
+    cudaFuncSetAttribute(gwm::k_gemm<BN, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  dim3 grid((N + BN - 1) / BN, (M + gwm::kBM - 1) / gwm::kBM);
+  gwm::k_gemm<BN, kStages><<<grid, gwm::kThreads, smem, n->stream>>>(ma, mb, M, N, K, ep, n->status);
   GWM_CUDA(n, cudaGetLastError());
   return GW_OK;
+}
+
+// C[M x N] = A[M x K] * B[N x K]^T with the given epilogue.  Small M takes
+// narrow tiles so that more CTAs share the K loop.
+static int gemm(gwm_net* n, const bf16* A, const bf16* B, int M, int N, int K, const gwm::Epilogue& ep) {
+  if (K % 8 != 0) return gwm_fail(n, GW_ERR_ARG, "GEMM K must be a multiple of 8");
+  const int tiles_m = (M + gwm::kBM - 1) / gwm::kBM;
+  if (N <= 64 || tiles_m * ((N + 127) / 128) < 64) return launch_gemm<64>(n, A, B, M, N, K, ep);
+  if (N <= 128 || tiles_m * ((N + 255) / 256) < 64) return launch_gemm<128>(n, A, B, M, N, K, ep);
+  return launch_gemm<256>(n, A, B, M, N, K, ep);
 }
 
 static int check_status(gwm_net* n) {
@@ -495,6 +846,10 @@ extern "C" int gwm_destroy(gwm_net* n) {
   cudaSetDevice(n->device);
   cudaStreamSynchronize(n->stream);
   for (void* p : n->allocs) cudaFree(p);
+  cudaFree(n->train_x);
+  cudaFree(n->train_t);
+  cudaFree(n->h_tab);
+  chain_free(n->chain);
   cudaStreamDestroy(n->stream);
   delete n;
   return GW_OK;
@@ -557,13 +912,22 @@ static int forward(gwm_net* n, int B) {
   return GW_OK;
 }
 
+static dim3 tiles32(int rows, int cols) { return dim3((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32)); }
+
+// Input rows to BF16 (and transposed) for the first GEMM; row r is perm[r] of x (perm null: r).
+// The transposed copy feeds the weight gradient of the first layer only.
+static int stage_input(gwm_net* n, const float* x, const int32_t* perm, int B, bool transposed = true) {
+  gwm::k_rows_to_bf16<<<tiles32(B, n->dims[0]), dim3(32, 8), 0, n->stream>>>(
+      x, perm, B, n->dims[0], n->h[0], transposed ? n->ht[0] : nullptr, B);
+  GWM_CUDA(n, cudaGetLastError());
+  return GW_OK;
+}
+
 static int load_input(gwm_net* n, const float* x, int B, bool device_ptr) {
   const size_t cnt = (size_t)B * n->dims[0];
   GWM_CUDA(n, cudaMemcpyAsync(n->xin, x, sizeof(float) * cnt,
                               device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, n->stream));
-  gwm::k_to_bf16<<<(unsigned)((cnt + 255) / 256), 256, 0, n->stream>>>(n->xin, B, n->dims[0], n->h[0], n->ht[0], B);
-  GWM_CUDA(n, cudaGetLastError());
-  return GW_OK;
+  return stage_input(n, n->xin, nullptr, B);
 }
 
 // Forward pass of B inputs x [B x dims[0]] (FP32, host or device) into
@@ -589,7 +953,7 @@ static int backward(gwm_net* n, int B) {
     e1.out_f32 = n->gw_[l];
     int rc = gemm(n, n->dzt[l], n->ht[l], n->dims[l + 1], n->dims[l], B, e1);
     if (rc) return rc;
-    gwm::k_colsum<<<(n->dims[l + 1] + 255) / 256, 256, 0, n->stream>>>(n->dz[l], B, n->dims[l + 1], n->gb[l]);
+    gwm::k_colsum<<<(n->dims[l + 1] + 31) / 32, dim3(32, 16), 0, n->stream>>>(n->dz[l], B, n->dims[l + 1], n->gb[l]);
     GWM_CUDA(n, cudaGetLastError());
     if (l > 0) {
       // dz_{l-1} = (dz_l W_l) * silu'(z_{l-1}) : [B x dims[l]], K = dims[l+1]
@@ -605,15 +969,39 @@ static int backward(gwm_net* n, int B) {
   return GW_OK;
 }
 
+// Loss and output gradient against targets t (rows perm[r] when perm is set);
+// adds scale * loss into *loss.
+static int mse(gwm_net* n, const float* t, const int32_t* perm, int B, float* loss, float scale) {
+  const int L = n->n_layers, C = n->dims[L];
+  gwm::k_mse<<<tiles32(B, C), dim3(32, 8), 0, n->stream>>>(n->z[L - 1], t, perm, B, C, n->dz[L - 1], n->dzt[L - 1],
+                                                            B, loss, scale);
+  GWM_CUDA(n, cudaGetLastError());
+  return GW_OK;
+}
+
 static int loss_and_grad(gwm_net* n, const float* t, int B, bool device_ptr) {
   const int L = n->n_layers, C = n->dims[L];
   const size_t cnt = (size_t)B * C;
   GWM_CUDA(n, cudaMemcpyAsync(n->target, t, sizeof(float) * cnt,
                               device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, n->stream));
   GWM_CUDA(n, cudaMemsetAsync(n->loss, 0, sizeof(float), n->stream));
-  gwm::k_mse<<<(unsigned)((cnt + 255) / 256), 256, 0, n->stream>>>(n->z[L - 1], n->target, B, C, n->dz[L - 1],
-                                                                    n->dzt[L - 1], B, n->loss);
-  GWM_CUDA(n, cudaGetLastError());
+  return mse(n, n->target, nullptr, B, n->loss, 1.f);
+}
+
+// One Adam update of every layer with learning rate lr.
+static int adam_all(gwm_net* n, float lr) {
+  n->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - powf(b1, (float)n->step), c2 = 1.f - powf(b2, (float)n->step);
+  for (int l = 0; l < n->n_layers; ++l) {
+    const int rows = n->dims[l + 1], cols = n->dims[l];
+    const int nw = rows * cols;
+    gwm::k_adam<<<(nw + 255) / 256, 256, 0, n->stream>>>(n->w[l], n->gw_[l], n->mw[l], n->vw[l], nw, rows, cols, lr,
+                                                         b1, b2, 1e-8f, c1, c2, n->wb[l], n->wt[l]);
+    gwm::k_adam<<<(rows + 255) / 256, 256, 0, n->stream>>>(n->b[l], n->gb[l], n->mb[l], n->vb[l], rows, 0, 1, lr,
+                                                           b1, b2, 1e-8f, c1, c2, nullptr, nullptr);
+    GWM_CUDA(n, cudaGetLastError());
+  }
   return GW_OK;
 }
 
@@ -649,19 +1037,8 @@ extern "C" int gwm_train_step(gwm_net* n, const float* x, const float* t, int32_
   if (!rc) rc = forward(n, B);
   if (!rc) rc = loss_and_grad(n, t, B, device_ptrs != 0);
   if (!rc) rc = backward(n, B);
+  if (!rc) rc = adam_all(n, lr);
   if (rc) return rc;
-  n->step += 1;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.f - powf(b1, (float)n->step), c2 = 1.f - powf(b2, (float)n->step);
-  for (int l = 0; l < n->n_layers; ++l) {
-    const int rows = n->dims[l + 1], cols = n->dims[l];
-    const int nw = rows * cols;
-    gwm::k_adam<<<(nw + 255) / 256, 256, 0, n->stream>>>(n->w[l], n->gw_[l], n->mw[l], n->vw[l], nw, rows, cols, lr,
-                                                         b1, b2, 1e-8f, c1, c2, n->wb[l], n->wt[l]);
-    gwm::k_adam<<<(rows + 255) / 256, 256, 0, n->stream>>>(n->b[l], n->gb[l], n->mb[l], n->vb[l], rows, 0, 1, lr,
-                                                           b1, b2, 1e-8f, c1, c2, nullptr, nullptr);
-    GWM_CUDA(n, cudaGetLastError());
-  }
   if (loss) {
     GWM_CUDA(n, cudaMemcpyAsync(loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, n->stream));
   }
@@ -697,34 +1074,130 @@ extern "C" int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, in
 // ---------------------------------------------------------------------------
 // Surrogate head: standardisation, affine base, output scaling, rate -> LLH.
 // ---------------------------------------------------------------------------
+static gwm::Head head_view(const gwm_net* n) {
+  gwm::Head h{};
+  h.din = n->dims[0];
+  h.nb = n->dims[n->n_layers];
+  h.nodes = n->h_nodes;
+  h.lim = n->h_lim;
+  h.tab = n->h_tab;
+  h.b0 = n->h_b0;
+  h.mu = n->h_mu;
+  h.sd = n->h_sd;
+  h.r_w = n->h_has_rw ? n->h_rw : nullptr;
+  h.r_b = n->h_rb;
+  return h;
+}
+
+// Buffers of the head and of gwm_predict; the base table is (re)sized to tab_elems.
+static int head_alloc(gwm_net* n, size_t tab_elems) {
+  const int din = n->dims[0], nb = n->dims[n->n_layers], Bm = n->batch_max;
+  if (!n->has_head) {
+    int rc = gwm_alloc(n, &n->h_mean, din) | gwm_alloc(n, &n->h_scale, din) | gwm_alloc(n, &n->h_b0, nb) |
+             gwm_alloc(n, &n->h_mu, nb) | gwm_alloc(n, &n->h_sd, nb) | gwm_alloc(n, &n->h_rb, nb) |
+             gwm_alloc(n, &n->h_rw, (size_t)din * nb) | gwm_alloc(n, &n->h_data, nb) |
+             gwm_alloc(n, &n->h_theta, (size_t)Bm * din) | gwm_alloc(n, &n->h_sums, (size_t)Bm * nb) |
+             gwm_alloc(n, &n->h_sums2, (size_t)Bm * nb) | gwm_alloc(n, &n->h_llh, Bm) |
+             gwm_alloc(n, &n->h_logr, (size_t)Bm * nb) | gwm_alloc(n, &n->h_part, (size_t)Bm * ((nb + 31) / 32));
+    if (rc) return rc;
+    n->has_head = true;
+  }
+  if (n->h_tab_elems != tab_elems) {
+    GWM_CUDA(n, cudaStreamSynchronize(n->stream));
+    cudaFree(n->h_tab);
+    n->h_tab = nullptr;
+    n->h_tab_elems = 0;
+    if (cudaMalloc(&n->h_tab, sizeof(float) * tab_elems) != cudaSuccess) {
+      cudaGetLastError();
+      n->h_tab = nullptr;
+      return gwm_fail(n, GW_ERR_NOMEM, "cudaMalloc failed (head table)");
+    }
+    n->h_tab_elems = tab_elems;
+  }
+  return GW_OK;
+}
+
+// Uploads the parts shared by both head forms.
+static int head_common(gwm_net* n, const float* in_mean, const float* in_scale, const float* base_b,
+                       const float* out_mu, const float* out_sd, const float* ratio_w, const double* data) {
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  GWM_CUDA(n, cudaMemcpy(n->h_mean, in_mean, sizeof(float) * din, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_scale, in_scale, sizeof(float) * din, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_b0, base_b, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_mu, out_mu, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_sd, out_sd, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_data, data, sizeof(double) * nb, cudaMemcpyHostToDevice));
+  n->h_has_rw = ratio_w != nullptr;
+  if (ratio_w) {
+    // [nb x din] -> [din x nb]
+    std::vector<float> rt((size_t)din * nb);
+    for (int b = 0; b < nb; ++b)
+      for (int k = 0; k < din; ++k) rt[(size_t)k * nb + b] = ratio_w[(size_t)b * din + k];
+    GWM_CUDA(n, cudaMemcpy(n->h_rw, rt.data(), sizeof(float) * rt.size(), cudaMemcpyHostToDevice));
+  }
+  return GW_OK;
+}
+
 extern "C" int gwm_set_head(gwm_net* n, const float* in_mean, const float* in_scale, const float* base_w,
                             const float* base_b, const float* out_mu, const float* out_sd, const float* ratio,
                             const double* data) {
   if (!n || !in_mean || !in_scale || !base_w || !base_b || !out_mu || !out_sd || !ratio || !data) return GW_ERR_ARG;
   GWM_CUDA(n, cudaSetDevice(n->device));
-  const int din = n->dims[0], nb = n->dims[n->n_layers], Bm = n->batch_max;
-  if (!n->has_head) {
-    int rc = gwm_alloc(n, &n->h_mean, din) | gwm_alloc(n, &n->h_scale, din) |
-             gwm_alloc(n, &n->h_wt, (size_t)din * nb) | gwm_alloc(n, &n->h_b0, nb) | gwm_alloc(n, &n->h_mu, nb) |
-             gwm_alloc(n, &n->h_sd, nb) | gwm_alloc(n, &n->h_ratio, nb) | gwm_alloc(n, &n->h_data, nb) |
-             gwm_alloc(n, &n->h_theta, (size_t)Bm * din) | gwm_alloc(n, &n->h_sums, (size_t)Bm * nb) |
-             gwm_alloc(n, &n->h_sums2, (size_t)Bm * nb) | gwm_alloc(n, &n->h_llh, Bm) |
-             gwm_alloc(n, &n->h_logr, (size_t)Bm * nb);
-    if (rc) return rc;
-    n->has_head = true;
-  }
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  int rc = head_alloc(n, (size_t)din * nb);
+  if (rc) return rc;
   // base_w arrives as [nb x din]; stored transposed [din x nb] for the head kernel
-  std::vector<float> wt((size_t)din * nb);
+  std::vector<float> wt((size_t)din * nb), lr(nb);
   for (int b = 0; b < nb; ++b)
     for (int k = 0; k < din; ++k) wt[(size_t)k * nb + b] = base_w[(size_t)b * din + k];
-  GWM_CUDA(n, cudaMemcpy(n->h_mean, in_mean, sizeof(float) * din, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_scale, in_scale, sizeof(float) * din, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_wt, wt.data(), sizeof(float) * wt.size(), cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_b0, base_b, sizeof(float) * nb, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_mu, out_mu, sizeof(float) * nb, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_sd, out_sd, sizeof(float) * nb, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_ratio, ratio, sizeof(float) * nb, cudaMemcpyHostToDevice));
-  GWM_CUDA(n, cudaMemcpy(n->h_data, data, sizeof(double) * nb, cudaMemcpyHostToDevice));
+  for (int b = 0; b < nb; ++b) lr[b] = ratio[b] > 0.f ? logf(ratio[b]) : -1e30f;
+  GWM_CUDA(n, cudaMemcpy(n->h_tab, wt.data(), sizeof(float) * wt.size(), cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_rb, lr.data(), sizeof(float) * nb, cudaMemcpyHostToDevice));
+  n->h_nodes = 0;
+  n->h_lim = 0.f;
+  return head_common(n, in_mean, in_scale, base_b, out_mu, out_sd, nullptr, data);
+}
+
+extern "C" int gwm_set_head_additive(gwm_net* n, const float* in_mean, const float* in_scale, int32_t nodes,
+                                     float lim, const float* base_tab, const float* base_b, const float* out_mu,
+                                     const float* out_sd, const float* ratio_w, const float* ratio_b,
+                                     const double* data) {
+  if (!n || !in_mean || !in_scale || !base_tab || !base_b || !out_mu || !out_sd || !ratio_b || !data || nodes < 2 ||
+      nodes > 4096 || !(lim > 0.f))
+    return gwm_fail(n, GW_ERR_ARG, "gwm_set_head_additive: bad arguments");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  const size_t te = (size_t)din * nodes * nb;
+  int rc = head_alloc(n, te);
+  if (rc) return rc;
+  GWM_CUDA(n, cudaMemcpy(n->h_tab, base_tab, sizeof(float) * te, cudaMemcpyHostToDevice));
+  GWM_CUDA(n, cudaMemcpy(n->h_rb, ratio_b, sizeof(float) * nb, cudaMemcpyHostToDevice));
+  n->h_nodes = nodes;
+  n->h_lim = lim;
+  return head_common(n, in_mean, in_scale, base_b, out_mu, out_sd, ratio_w, data);
+}
+
+// Fused head + likelihood of the first C rows of the network's output (xin
+// holds their standardised inputs): h_llh [C]; with `outputs`, h_sums,
+// h_sums2 and h_logr too.
+static int head_llh(gwm_net* n, int C, int llh_type, bool outputs) {
+  const int nb = n->dims[n->n_layers], L = n->n_layers;
+  constexpr int kPPT = 2;
+  const int nbx = (nb + 31) / 32;
+  dim3 grid(nbx, (C + 8 * kPPT - 1) / (8 * kPPT));
+  const size_t shm = (size_t)8 * kPPT * n->dims[0] * 12;
+  if (shm > 48 * 1024) {
+    static std::once_flag once;
+    std::call_once(once, []() {
+      cudaFuncSetAttribute(gwm::k_head_llh<kPPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (shm > 200 * 1024) return gwm_fail(n, GW_ERR_LIMIT, "surrogate head: too many inputs");
+  }
+  gwm::k_head_llh<kPPT><<<grid, dim3(32, 8), shm, n->stream>>>(
+      head_view(n), n->xin, n->z[L - 1], C, n->h_data, llh_type, n->h_part, outputs ? n->h_sums : nullptr,
+      outputs ? n->h_sums2 : nullptr, outputs ? n->h_logr : nullptr);
+  gwm::k_llh_finish<<<(C + 7) / 8, 256, 0, n->stream>>>(n->h_part, nbx, C, n->h_llh);
+  GWM_CUDA(n, cudaGetLastError());
   return GW_OK;
 }
 
@@ -742,20 +1215,450 @@ extern "C" int gwm_predict(gwm_net* n, const double* theta, int32_t B, int32_t l
   GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, theta, sizeof(double) * (size_t)B * din, cudaMemcpyHostToDevice, n->stream));
   gwm::k_standardize<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->h_theta, Bp, din,
                                                                                      n->h_mean, n->h_scale, n->xin);
-  gwm::k_to_bf16<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->xin, Bp, din, n->h[0],
-                                                                                    n->ht[0], Bp);
-  GWM_CUDA(n, cudaGetLastError());
-  int rc = forward(n, Bp);
+  int rc = stage_input(n, n->xin, nullptr, Bp, false);
   if (rc) return rc;
-  gwm::k_head<<<dim3((nb + 255) / 256, B), 256, 0, n->stream>>>(n->xin, din, n->h_wt, n->h_b0, n->h_mu, n->h_sd,
-                                                                 n->h_ratio, n->z[L - 1], nb, n->h_sums, n->h_sums2,
-                                                                 log_rates ? n->h_logr : nullptr);
   GWM_CUDA(n, cudaGetLastError());
-  rc = gw_llh_noalloc(n->h_sums, n->h_sums2, n->h_data, nb, B, llh_type, n->h_llh, n->stream);
-  if (rc) return gwm_fail(n, rc, "gwm_predict: likelihood reduction failed");
+  rc = forward(n, Bp);
+  if (rc) return rc;
+  rc = head_llh(n, B, llh_type, log_rates != nullptr);
+  if (rc) return rc;
   GWM_CUDA(n, cudaMemcpyAsync(llh, n->h_llh, sizeof(double) * B, cudaMemcpyDeviceToHost, n->stream));
   if (log_rates)
     GWM_CUDA(n, cudaMemcpyAsync(log_rates, n->h_logr, sizeof(double) * (size_t)B * nb, cudaMemcpyDeviceToHost,
                                 n->stream));
+  return check_status(n);
+}
+
+// ---------------------------------------------------------------------------
+// Training set on the device and the training loop.
+// ---------------------------------------------------------------------------
+extern "C" int gwm_train_reserve(gwm_net* n, int64_t n_max) {
+  if (!n || n_max < 8) return gwm_fail(n, GW_ERR_ARG, "gwm_train_reserve: n_max must be >= 8");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  GWM_CUDA(n, cudaStreamSynchronize(n->stream));
+  cudaFree(n->train_x);
+  cudaFree(n->train_t);
+  n->train_x = n->train_t = nullptr;
+  n->train_n = n->train_max = 0;
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  if (cudaMalloc(&n->train_x, sizeof(float) * (size_t)n_max * din) != cudaSuccess ||
+      cudaMalloc(&n->train_t, sizeof(float) * (size_t)n_max * nb) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(n->train_x);
+    cudaFree(n->train_t);
+    n->train_x = n->train_t = nullptr;
+    return gwm_fail(n, GW_ERR_NOMEM, "gwm_train_reserve: cudaMalloc failed");
+  }
+  n->train_max = n_max;
+  return GW_OK;
+}
+
+extern "C" int gwm_train_size(gwm_net* n, int64_t* count) {
+  if (!n || !count) return GW_ERR_ARG;
+  *count = n->train_n;
+  return GW_OK;
+}
+
+// Standardises h_theta rows and turns h_sums rows into targets at the end of
+// the training set (the head must be set).
+static int append_rows(gwm_net* n, int K) {
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  float* x = n->train_x + (size_t)n->train_n * din;
+  gwm::k_standardize<<<(unsigned)(((size_t)K * din + 255) / 256), 256, 0, n->stream>>>(n->h_theta, K, din, n->h_mean,
+                                                                                    n->h_scale, x);
+  gwm::k_target<<<dim3((nb + 255) / 256, K), 256, 0, n->stream>>>(head_view(n), x, n->h_sums,
+                                                                  n->train_t + (size_t)n->train_n * nb);
+  GWM_CUDA(n, cudaGetLastError());
+  n->train_n += K;
+  return GW_OK;
+}
+
+static int append_check(gwm_net* n, const double* theta, int K, const char* who) {
+  if (!n || !theta || K < 1 || K > n->batch_max) return gwm_fail(n, GW_ERR_ARG, who);
+  if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "training targets need the head (gwm_set_head) first");
+  if (n->train_n + K > n->train_max) return gwm_fail(n, GW_ERR_LIMIT, "training set full (gwm_train_reserve)");
+  return GW_OK;
+}
+
+// Appends K points theta [K x dims[0]] (host FP64) with their bin sums
+// [K x dims[L]] (FP64, host, or device memory when sums_on_device != 0).
+extern "C" int gwm_train_append(gwm_net* n, const double* theta, const double* sums, int32_t K,
+                                int32_t sums_on_device) {
+  int rc = append_check(n, theta, K, "gwm_train_append: bad arguments");
+  if (rc) return rc;
+  if (!sums) return gwm_fail(n, GW_ERR_ARG, "gwm_train_append: sums missing");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, theta, sizeof(double) * (size_t)K * din, cudaMemcpyHostToDevice, n->stream));
+  GWM_CUDA(n, cudaMemcpyAsync(n->h_sums, sums, sizeof(double) * (size_t)K * nb,
+                              sums_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, n->stream));
+  rc = append_rows(n, K);
+  if (rc) return rc;
+  GWM_CUDA(n, cudaStreamSynchronize(n->stream));
+  return GW_OK;
+}
+
+// Appends K points theta [K x dims[0]] (host FP64) reweighted exactly by the
+// engine e on the network's stream; nothing leaves the device.  The engine's
+// parameter count must equal dims[0], its bin count dims[L], and K <= its k_max.
+extern "C" int gwm_train_append_eval(gwm_net* n, gw_engine* e, const double* theta, int32_t K) {
+  int rc = append_check(n, theta, K, "gwm_train_append_eval: bad arguments");
+  if (rc) return rc;
+  if (!e) return gwm_fail(n, GW_ERR_ARG, "gwm_train_append_eval: no engine");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0];
+  GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, theta, sizeof(double) * (size_t)K * din, cudaMemcpyHostToDevice, n->stream));
+  rc = gw_eval_device(e, n->h_theta, K, n->h_sums, n->h_sums2, nullptr, nullptr, (void*)n->stream);
+  if (rc) {
+    char buf[256];
+    gw_last_error(e, buf, sizeof(buf));
+    n->err = std::string("gwm_train_append_eval: engine: ") + buf;
+    return rc;
+  }
+  return append_rows(n, K);
+}
+
+// Trains on the device-resident set: `epochs` passes of floor(count / batch)
+// Adam steps over a seeded permutation per epoch, learning rate cosine-decayed
+// from lr0 to lr_min over all steps.  No host synchronisation between steps;
+// losses[e] = mean training loss of epoch e (optional).
+extern "C" int gwm_train_epochs(gwm_net* n, int32_t epochs, int32_t batch, float lr0, float lr_min, uint64_t seed,
+                                float* losses) {
+  if (!n || epochs < 1 || batch < 8 || batch % 8 || batch > n->batch_max)
+    return gwm_fail(n, GW_ERR_ARG, "gwm_train_epochs: bad epochs or batch");
+  if (n->train_n < batch) return gwm_fail(n, GW_ERR_STATE, "gwm_train_epochs: fewer training points than one batch");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int64_t N = n->train_n;
+  const int64_t spe = N / batch, total = (int64_t)epochs * spe;
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  // permutations of all epochs, drawn on the host (splitmix64 + Fisher-Yates)
+  std::vector<int32_t> perm((size_t)epochs * N);
+  uint64_t st = seed;
+  auto next = [&st]() {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  for (int e = 0; e < epochs; ++e) {
+    int32_t* p = perm.data() + (size_t)e * N;
+    for (int64_t i = 0; i < N; ++i) p[i] = (int32_t)i;
+    for (int64_t i = N - 1; i > 0; --i) {
+      const int64_t j = (int64_t)(next() % (uint64_t)(i + 1));
+      std::swap(p[i], p[j]);
+    }
+  }
+  int32_t* d_perm = nullptr;
+  float* d_loss = nullptr;
+  if (cudaMalloc(&d_perm, sizeof(int32_t) * perm.size()) != cudaSuccess ||
+      cudaMalloc(&d_loss, sizeof(float) * epochs) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d_perm);
+    return gwm_fail(n, GW_ERR_NOMEM, "gwm_train_epochs: cudaMalloc failed");
+  }
+  int rc = GW_OK;
+  if (cudaMemcpyAsync(d_perm, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice, n->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(d_loss, 0, sizeof(float) * epochs, n->stream) != cudaSuccess)
+    rc = gwm_fail(n, GW_ERR_CUDA, "gwm_train_epochs: copy failed");
+  const float inv_spe = 1.f / (float)spe;
+  for (int64_t s = 0; s < total && rc == GW_OK; ++s) {
+    const int64_t e = s / spe, j = s % spe;
+    const int32_t* p = d_perm + e * N + j * batch;
+    const double c = std::cos(M_PI * (double)s / (double)total);
+    const float lr = (float)(lr_min + 0.5 * (lr0 - lr_min) * (1.0 + c));
+    rc = stage_input(n, n->train_x, p, batch);
+    if (!rc) rc = forward(n, batch);
+    if (!rc) rc = mse(n, n->train_t, p, batch, d_loss + e, inv_spe);
+    if (!rc) rc = backward(n, batch);
+    if (!rc) rc = adam_all(n, lr);
+  }
+  (void)din;
+  (void)nb;
+  if (rc == GW_OK) rc = check_status(n);
+  if (rc == GW_OK && losses &&
+      cudaMemcpy(losses, d_loss, sizeof(float) * epochs, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = gwm_fail(n, GW_ERR_CUDA, "gwm_train_epochs: loss copy failed");
+  cudaStreamSynchronize(n->stream);
+  cudaFree(d_perm);
+  cudaFree(d_loss);
+  return rc;
+}
+
+// Copies rows [first, first + count) of the training set to the host:
+// x [count x dims[0]] standardised inputs, t [count x dims[L]] targets.
+extern "C" int gwm_train_read(gwm_net* n, int64_t first, int32_t count, float* x, float* t) {
+  if (!n || first < 0 || count < 0 || first + count > n->train_n) return gwm_fail(n, GW_ERR_ARG, "gwm_train_read: range");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  GWM_CUDA(n, cudaStreamSynchronize(n->stream));
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
+  if (x && count)
+    GWM_CUDA(n, cudaMemcpy(x, n->train_x + (size_t)first * din, sizeof(float) * (size_t)count * din,
+                           cudaMemcpyDeviceToHost));
+  if (t && count)
+    GWM_CUDA(n, cudaMemcpy(t, n->train_t + (size_t)first * nb, sizeof(float) * (size_t)count * nb,
+                           cudaMemcpyDeviceToHost));
+  return GW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Surrogate random-walk Metropolis sub-chains on the device: stage 1 of the
+// delayed-acceptance sampler.  Per chain c and sub-step s:
+//   prop = phi + L n,  n ~ N(0, I) (counter-based hash of (seed, s, c, k));
+//   f(prop) = surrogate statistical LLH + (prop - m)^T C^-1 (prop - m);
+//   accept when log u < -(f(prop) - f(phi)) / 2, u from the same hash.
+// The surrogate of a point depends on that point alone (row-independent GEMM
+// tiles, fixed-order reductions), so f is a fixed function of the point.
+// ---------------------------------------------------------------------------
+namespace gwm {
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ uint64_t hash4(uint64_t seed, uint64_t step, uint64_t chain, uint64_t k) {
+  uint64_t h = mix64(seed + 0x9E3779B97F4A7C15ull);
+  h = mix64(h ^ (step * 0xD1B54A32D192ED03ull));
+  h = mix64(h ^ (chain * 0xABC98388FB8FAC03ull));
+  return mix64(h ^ (k * 0x8CB92BA72F3D8DD7ull));
+}
+
+// uniform in (0, 1), 53 bits
+__device__ __forceinline__ double u01(uint64_t h) { return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+// Block per chain: n[k] standard normals (Box-Muller on hash pairs, FP64),
+// then prop[c][p] = phi[c][p] + sum_{k<=p} L[p][k] n[k] with the increment in
+// FP32 (Lt = L transposed, so that thread p reads column p coalesced).  The
+// increment depends on n alone, so the proposal stays symmetric.
+__global__ void k_propose(const double* __restrict__ phi, int P, const float* __restrict__ Lt, uint64_t seed,
+                          uint64_t step, double* __restrict__ prop) {
+  extern __shared__ float nrm[];
+  const int c = blockIdx.x;
+  for (int k2 = threadIdx.x; 2 * k2 < P; k2 += blockDim.x) {
+    const double u1 = u01(hash4(seed, step, c, 2 * k2));
+    const double u2 = u01(hash4(seed, step, c, 2 * k2 + 1));
+    const double r = sqrt(-2.0 * log(u1));
+    double sn, cs;
+    sincospi(2.0 * u2, &sn, &cs);
+    nrm[2 * k2] = (float)(r * cs);
+    if (2 * k2 + 1 < P) nrm[2 * k2 + 1] = (float)(r * sn);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    int k = 0;
+    for (; k + 4 <= p + 1; k += 4) {
+      a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
+      a1 = fmaf(Lt[(size_t)(k + 1) * P + p], nrm[k + 1], a1);
+      a2 = fmaf(Lt[(size_t)(k + 2) * P + p], nrm[k + 2], a2);
+      a3 = fmaf(Lt[(size_t)(k + 3) * P + p], nrm[k + 3], a3);
+    }
+    for (; k <= p; ++k) a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
+    prop[(size_t)c * P + p] = phi[(size_t)c * P + p] + (double)((a0 + a1) + (a2 + a3));
+  }
+}
+
+// Block per chain: pen[c] = d^T C^-1 d, d = x[c] - m, in FP32 (C^-1 symmetric,
+// read by columns), fixed-order reduction.
+__global__ void k_penalty(const double* __restrict__ x, int P, const double* __restrict__ m,
+                          const float* __restrict__ icov, double* __restrict__ pen) {
+  extern __shared__ float shf[];
+  float* d = shf;          // [P]
+  float* part = shf + P;   // [blockDim.x]
+  const int c = blockIdx.x;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) d[p] = (float)(x[(size_t)c * P + p] - m[p]);
+  __syncthreads();
+  float acc = 0.f;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
+    int k = 0;
+    for (; k + 4 <= P; k += 4) {
+      u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+      u1 = fmaf(icov[(size_t)(k + 1) * P + p], d[k + 1], u1);
+      u2 = fmaf(icov[(size_t)(k + 2) * P + p], d[k + 2], u2);
+      u3 = fmaf(icov[(size_t)(k + 3) * P + p], d[k + 3], u3);
+    }
+    for (; k < P; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+    acc = fmaf(d[p], (u0 + u1) + (u2 + u3), acc);
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)blockDim.x; ++i) s += (double)part[i];
+    pen[c] = s;
+  }
+}
+
+// Block per chain: Metropolis decision on f = llh + pen (pen optional); on
+// acceptance the proposal row replaces phi and f.  step == ~0 marks the
+// initial evaluation (f taken unconditionally).
+__global__ void k_accept(const double* __restrict__ prop, const double* __restrict__ llh,
+                         const double* __restrict__ pen, int P, uint64_t seed, uint64_t step, int first,
+                         double* __restrict__ phi, double* __restrict__ f, int32_t* __restrict__ n_acc) {
+  const int c = blockIdx.x;
+  const double fn = llh[c] + (pen ? pen[c] : 0.0);
+  bool take;
+  if (first) {
+    take = false;
+  } else {
+    const double u = u01(hash4(seed, step, c, 0xFFFFFFFFull));
+    const double d = -(fn - f[c]) * 0.5;
+    take = log(u) < d;  // NaN proposals are rejected
+  }
+  if (first) {
+    if (threadIdx.x == 0) f[c] = fn;
+    return;
+  }
+  if (!take) return;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) phi[(size_t)c * P + p] = prop[(size_t)c * P + p];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    f[c] = fn;
+    n_acc[c] += 1;
+  }
+}
+
+}  // namespace
+}  // namespace gwm
+
+// Chain state on the device (sized at gwm_set_chain).
+struct gwm_chain_state {
+  int P = 0;
+  bool prior = false;
+  float *Lt = nullptr, *icov = nullptr;
+  double *m = nullptr, *phi = nullptr, *f = nullptr, *pen = nullptr;
+  int32_t* nacc = nullptr;
+};
+
+static void chain_free(gwm_chain_state* s) {
+  if (!s) return;
+  cudaFree(s->Lt);
+  cudaFree(s->m);
+  cudaFree(s->icov);
+  cudaFree(s->phi);
+  cudaFree(s->f);
+  cudaFree(s->pen);
+  cudaFree(s->nacc);
+  delete s;
+}
+
+// Evaluates the surrogate statistical LLH of the first C rows of h_theta
+// (device) into h_llh.  Rows C..roundup(C, 8) of h_theta must be finite.
+static int surrogate_llh_device(gwm_net* n, int C, int llh_type) {
+  const int din = n->dims[0];
+  const int Bp = ((C + 7) / 8) * 8;
+  gwm::k_standardize<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->h_theta, Bp, din,
+                                                                                     n->h_mean, n->h_scale, n->xin);
+  int rc = stage_input(n, n->xin, nullptr, Bp, false);
+  if (!rc) rc = forward(n, Bp);
+  if (rc) return rc;
+  return head_llh(n, C, llh_type, false);
+}
+
+// Proposal Cholesky factor L [P x P] (lower, row-major, host FP64) and the
+// Gaussian prior (mean [P], inverse covariance [P x P]; both null for none)
+// of the sub-chains; P == dims[0].  Room for up to batch_max chains.
+extern "C" int gwm_set_chain(gwm_net* n, const double* prop_chol, const double* prior_mean,
+                             const double* prior_icov) {
+  if (!n || !prop_chol || ((prior_mean == nullptr) != (prior_icov == nullptr)))
+    return gwm_fail(n, GW_ERR_ARG, "gwm_set_chain: bad arguments");
+  if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_set_chain: gwm_set_head first");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  GWM_CUDA(n, cudaStreamSynchronize(n->stream));
+  const int P = n->dims[0], Cm = n->batch_max;
+  gwm_chain_state* s = n->chain;
+  if (!s) {
+    s = new gwm_chain_state();
+    s->P = P;
+    bool ok = cudaMalloc(&s->Lt, sizeof(float) * P * P) == cudaSuccess &&
+              cudaMalloc(&s->m, sizeof(double) * P) == cudaSuccess &&
+              cudaMalloc(&s->icov, sizeof(float) * P * P) == cudaSuccess &&
+              cudaMalloc(&s->phi, sizeof(double) * (size_t)Cm * P) == cudaSuccess &&
+              cudaMalloc(&s->f, sizeof(double) * Cm) == cudaSuccess &&
+              cudaMalloc(&s->pen, sizeof(double) * Cm) == cudaSuccess &&
+              cudaMalloc(&s->nacc, sizeof(int32_t) * Cm) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      chain_free(s);
+      return gwm_fail(n, GW_ERR_NOMEM, "gwm_set_chain: cudaMalloc failed");
+    }
+    n->chain = s;
+  }
+  std::vector<float> f32((size_t)P * P);
+  for (int p = 0; p < P; ++p)
+    for (int k = 0; k < P; ++k) f32[(size_t)k * P + p] = (float)prop_chol[(size_t)p * P + k];
+  GWM_CUDA(n, cudaMemcpy(s->Lt, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+  s->prior = prior_mean != nullptr;
+  if (s->prior) {
+    // symmetric: C^-1 [k][p] read as column p; symmetrised in FP64 first
+    for (int p = 0; p < P; ++p)
+      for (int k = 0; k < P; ++k)
+        f32[(size_t)k * P + p] = (float)(0.5 * (prior_icov[(size_t)k * P + p] + prior_icov[(size_t)p * P + k]));
+    GWM_CUDA(n, cudaMemcpy(s->m, prior_mean, sizeof(double) * P, cudaMemcpyHostToDevice));
+    GWM_CUDA(n, cudaMemcpy(s->icov, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+  }
+  return GW_OK;
+}
+
+// Runs n_sub surrogate Metropolis steps for C chains from theta0 [C x P]
+// (host FP64) with surrogate values f0 [C] (stat LLH + prior penalty, host;
+// null: computed first, on the device).  Writes the end points phi [C x P],
+// their surrogate values fphi [C] and the accepted sub-steps n_acc [C].
+// n_sub == 0 with f0 == null evaluates the surrogate at theta0.
+extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, int32_t C, int32_t n_sub,
+                            int32_t llh_type, uint64_t seed, double* phi, double* fphi, int32_t* n_acc) {
+  if (!n || !theta0 || !phi || !fphi || C < 1 || C > n->batch_max || n_sub < 0)
+    return gwm_fail(n, GW_ERR_ARG, "gwm_substeps: bad arguments");
+  gwm_chain_state* s = n->chain;
+  if (!s || !n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_substeps: gwm_set_chain first");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int P = s->P;
+  const int Bp = ((C + 7) / 8) * 8;
+  const unsigned thr = P >= 256 ? 256 : (unsigned)(((P + 31) / 32) * 32);
+  const bool prior = s->prior;
+  const size_t sh_prop = sizeof(float) * (size_t)(P + 1);
+  const size_t sh_pen = sizeof(float) * ((size_t)P + thr);
+  GWM_CUDA(n, cudaMemcpyAsync(s->phi, theta0, sizeof(double) * (size_t)C * P, cudaMemcpyHostToDevice, n->stream));
+  GWM_CUDA(n, cudaMemsetAsync(s->nacc, 0, sizeof(int32_t) * C, n->stream));
+  // rows C..Bp of the staging buffer stay finite (zeros)
+  if (Bp > C)
+    GWM_CUDA(n, cudaMemsetAsync(n->h_theta + (size_t)C * P, 0, sizeof(double) * (size_t)(Bp - C) * P, n->stream));
+  int rc = GW_OK;
+  if (f0) {
+    GWM_CUDA(n, cudaMemcpyAsync(s->f, f0, sizeof(double) * C, cudaMemcpyHostToDevice, n->stream));
+  } else {
+    GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, s->phi, sizeof(double) * (size_t)C * P, cudaMemcpyDeviceToDevice,
+                                n->stream));
+    rc = surrogate_llh_device(n, C, llh_type);
+    if (rc) return rc;
+    if (prior) {
+      gwm::k_penalty<<<C, thr, sh_pen, n->stream>>>(s->phi, P, s->m, s->icov, s->pen);
+      GWM_CUDA(n, cudaGetLastError());
+    }
+    gwm::k_accept<<<C, thr, 0, n->stream>>>(s->phi, n->h_llh, prior ? s->pen : nullptr, P, seed, 0, 1, s->phi, s->f,
+                                          s->nacc);
+    GWM_CUDA(n, cudaGetLastError());
+  }
+  for (int st = 0; st < n_sub && rc == GW_OK; ++st) {
+    gwm::k_propose<<<C, thr, sh_prop, n->stream>>>(s->phi, P, s->Lt, seed, (uint64_t)st + 1, n->h_theta);
+    GWM_CUDA(n, cudaGetLastError());
+    rc = surrogate_llh_device(n, C, llh_type);
+    if (rc) break;
+    if (prior) {
+      gwm::k_penalty<<<C, thr, sh_pen, n->stream>>>(n->h_theta, P, s->m, s->icov, s->pen);
+      GWM_CUDA(n, cudaGetLastError());
+    }
+    gwm::k_accept<<<C, thr, 0, n->stream>>>(n->h_theta, n->h_llh, prior ? s->pen : nullptr, P, seed,
+                                          (uint64_t)st + 1, 0, s->phi, s->f, s->nacc);
+    GWM_CUDA(n, cudaGetLastError());
+  }
+  if (rc) return rc;
+  GWM_CUDA(n, cudaMemcpyAsync(phi, s->phi, sizeof(double) * (size_t)C * P, cudaMemcpyDeviceToHost, n->stream));
+  GWM_CUDA(n, cudaMemcpyAsync(fphi, s->f, sizeof(double) * C, cudaMemcpyDeviceToHost, n->stream));
+  if (n_acc) GWM_CUDA(n, cudaMemcpyAsync(n_acc, s->nacc, sizeof(int32_t) * C, cudaMemcpyDeviceToHost, n->stream));
   return check_status(n);
 }

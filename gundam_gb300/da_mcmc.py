@@ -1,134 +1,237 @@
 """Surrogate delayed-acceptance MCMC against plain-engine MCMC on one GPU.
 
     python -m gundam_gb300.da_mcmc [--events N] [--train N] [--epochs E]
-                                   [--chains C] [--steps S] [--n-sub M]
+                                   [--chains C] [--steps S] [--da-steps S]
+                                   [--n-sub M] [--region posterior|prior]
+                                   [--proposal adapted|prior]
 
-1. Training set: ``--train`` parameter draws from the prior with its
-   covariance inflated x1.5, reweighted exactly by the engine (FP32 dials,
-   FP64 sums); targets are log(sum of weights) per bin.
-2. Surrogate: affine least-squares base + BF16 MLP (P -> 512 -> 512 -> 512 -> B,
-   SiLU) on the residual, Adam with a cosine-decayed learning rate.
-3. Sampling: C chains of random-walk Metropolis with proposal covariance
-   2.38^2/P x prior covariance; "plain" evaluates every proposal exactly,
-   "delayed" runs n_sub surrogate steps per exact stage-2 correction.
-4. Reported: ESS/s (min and median over parameters, Geyer initial positive
-   sequence), stage-2 acceptance, the surrogate's likelihood error against the
-   exact one on held-out draws, and the posterior means / widths of the two
-   samplers in units of the posterior width.
+1. Fit: Gauss-Newton minimum of -2 log L and its Laplace covariance, from
+   batched engine launches (``fit.laplace``), as GUNDAM fits before sampling;
+   then an adaptive pilot of the plain sampler (``mcmc.adapt``) sets the
+   proposal covariance and scale, as SimpleMcmc's adaptive proposal does.
+2. Training set: ``--train`` parameter draws from the region (the pilot's
+   posterior mean and covariance, or the prior, with the covariance inflated
+   x1.5), reweighted exactly by the engine (FP32 dials, FP64 sums) on the
+   device; targets are log(sum of weights) per bin after an additive base (one
+   piecewise-linear function per parameter and bin) fitted by least squares on
+   a host-side subset, which also fits the model of sum(w^2).
+3. Surrogate: BF16 MLP (P -> 512 -> 512 -> 512 -> B, SiLU) on the residual,
+   Adam with a cosine-decayed learning rate, trained by libgw's own loop.
+4. Sampling: C chains of random-walk Metropolis from the pilot's final
+   states with the pilot's proposal (``--proposal prior``: 2.38^2/P x the
+   prior covariance from the fit's draws).  "plain" evaluates every proposal
+   exactly; "delayed" runs n_sub surrogate steps per chain on the device
+   (``Surrogate.substeps``) per exact stage-2 correction; "delayed_base_only"
+   is the same with the network's output set to zero (the base alone), which
+   shows what the network adds.
+5. Reported: ESS/s (min and median over parameters, multi-chain estimator
+   with Geyer's initial positive sequence, ``mcmc.ess``), stage-2 acceptance, the surrogate's likelihood error against the
+   exact one, and the delayed sampler's posterior means and widths against the
+   plain sampler's, in units of the posterior width and of their Monte Carlo
+   standard errors.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
 
 import numpy as np
 
 from . import _native as N
+from . import fit as fitmod
 from . import mcmc
 from .engine import Engine
-from .surrogate import Surrogate, training_data
+from .surrogate import Surrogate
 from .workload import Workload
 
 
-def penalty(wl, icov, th):
-    d = np.atleast_2d(th) - wl.prior_mean
-    return np.einsum("ij,jk,ik->i", d, icov, d)
+def penalty(mean, icov, th):
+    d = np.atleast_2d(th) - mean
+    return np.sum((d @ icov) * d, axis=1)
 
 
-def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2, config="c2", log=print,
-        precision="fp32", region="pilot", pilot_steps=200):
-    """region: where the training draws come from -- "prior" (the prior with
-    its covariance inflated x1.5) or "pilot" (a short plain-MCMC pilot run:
-    its sample mean with its sample covariance inflated x1.5)."""
+def _draws(rng, center, chol, n, inflate=1.0):
+    return center[None, :] + inflate * rng.standard_normal((n, center.shape[0])) @ chol.T
+
+
+def _sampler_stats(ch, seconds, burn):
+    e = mcmc.ess(ch, burn=burn)
+    return e, {"seconds": seconds, "ess_min": float(e.min()), "ess_median": float(np.median(e)),
+               "ess_per_s_min": float(e.min() / seconds), "ess_per_s_median": float(np.median(e) / seconds)}
+
+
+def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=2, config="c2", log=None,
+        precision="fp32", region="posterior", proposal="adapted", base_points=32768, nodes=8, batch=2048,
+        lr=1e-3, linear=True, max_error=20.0, adapt_cycles=6, adapt_steps=200, da_steps=None):
+    """Fit, adapt, train, then sample with both samplers from the same states
+    (``steps`` plain steps and ``da_steps`` (default: the same) delayed steps)."""
+    log = log or (lambda *_: None)
     t_all = time.perf_counter()
+    da_steps = da_steps or steps
     wl = Workload(config, n_events=events, seed=seed)
     llh_type = N.GW_LLH_BARLOW_BEESTON_OA2021 if config in ("c2", "c5") else N.GW_LLH_POISSON
-    eng = Engine.from_workload(wl, precision=precision, k_max=max(64, chains), llh_type=llh_type)
+    k = max(64, chains)
+    eng = Engine.from_workload(wl, precision=precision, k_max=k, llh_type=llh_type)
     eng.autotune(chains)
     icov = wl.prior_icov
+    P, B = wl.n_params, wl.n_bins
 
     def f_exact(th):
         out = np.empty(th.shape[0])
-        for s in range(0, th.shape[0], 64):
-            out[s:s + 64] = eng.eval(th[s:s + 64])[2]
+        for s in range(0, th.shape[0], k):
+            out[s:s + k] = eng.eval(th[s:s + k])[2]
         return out
 
-    L = mcmc.proposal_chol(wl.prior_cov)
-    th0 = wl.draw_points(chains, seed + 5, inflate=0.3)
-    # pilot / burn-in with the plain sampler (shared by both samplers below)
+    # 1. fit, then the adaptive pilot (proposal covariance and scale)
+    fr = fitmod.laplace(eng, wl.prior_mean, icov, log=log)
     t0 = time.perf_counter()
-    pilot = mcmc.plain(f_exact, th0, pilot_steps, L, seed=seed + 6)
-    t_pilot = time.perf_counter() - t0
-    th0 = pilot["chains"][-1].copy()
-    pil = pilot["chains"][pilot_steps // 2:].reshape(-1, wl.n_params)
-    t0 = time.perf_counter()
-    if region == "prior":
-        thetas, logs, ratio = training_data(eng, wl, train, seed=seed + 10, inflate=1.5)
+    rng0 = np.random.default_rng(seed + 5)
+    th_start = _draws(rng0, fr["theta"], np.linalg.cholesky(fr["cov"]), chains, 0.3)
+    if proposal == "adapted":
+        ad = mcmc.adapt(f_exact, th_start, fr["cov"], cycles=adapt_cycles, steps=adapt_steps, seed=seed + 6)
+        cov_post, scale = ad["cov"], ad["scale"]
+        th0 = ad["theta"]
+        post_samples = ad["chains"][adapt_steps // 2:].reshape(-1, P)
+        center = post_samples.mean(axis=0)
     else:
-        mean = pil.mean(0)
-        cov = np.cov(pil.T) + 1e-12 * np.eye(wl.n_params)
-        rng = np.random.default_rng(seed + 10)
-        thetas = mean + 1.5 * rng.standard_normal((train, wl.n_params)) @ np.linalg.cholesky(cov).T
-        logs = np.empty((train, wl.n_bins))
-        ratio = np.zeros(wl.n_bins)
-        for s0 in range(0, train, 64):
-            sums, sums2, _, _ = eng.eval(thetas[s0:s0 + 64])
-            logs[s0:s0 + 64] = np.log(np.maximum(sums, 1e-300))
-            ratio += (sums2 / np.maximum(sums, 1e-300)).sum(axis=0)
-        ratio /= train
-    t_data = time.perf_counter() - t0
-    sur = Surrogate(wl.n_params, wl.n_bins, batch_max=4096, seed=seed)
+        cov_post, scale = wl.prior_cov, 2.38 ** 2 / P
+        th0 = th_start
+        post_samples = None
+        center = fr["theta"]
+    t_adapt = time.perf_counter() - t0
+    log(f"pilot: {t_adapt:.2f} s, acceptance {ad['accept'] if proposal == 'adapted' else None}")
+    L = np.linalg.cholesky(scale * cov_post)
+
+    # 2. training set: base on a host-side pilot subset, then the device set
+    rng = np.random.default_rng(seed + 10)
+    if region == "posterior":
+        chol_r = np.linalg.cholesky(cov_post)
+    else:
+        center, chol_r = wl.prior_mean, np.linalg.cholesky(wl.prior_cov)
     t0 = time.perf_counter()
-    hist = sur.fit(thetas, logs, epochs=epochs, lr=1e-3, batch=min(2048, train))
+    n_b = min(base_points, train)
+    th_b = _draws(rng, center, chol_r, n_b, 1.5)
+    sums = np.empty((n_b, B))
+    lratio = np.empty((n_b, B))
+    for s in range(0, n_b, k):
+        a, b, _, _ = eng.eval(th_b[s:s + k])
+        sums[s:s + k] = a
+        lratio[s:s + k] = np.log(np.maximum(b, 1e-300)) - np.log(np.maximum(a, 1e-300))
+    t_base_data = time.perf_counter() - t0
+    sur = Surrogate(P, B, batch_max=4096, seed=seed)
+    t1 = time.perf_counter()
+    sur.fit_additive(th_b, np.log(np.maximum(sums, 1e-300)), log_ratio=lratio, nodes=nodes)
+    t_base_fit = time.perf_counter() - t1
+    del lratio
+    sur.attach(wl.data, None, llh_type)
+    sur.reserve(train)
+    sur.append(th_b, sums)
+    del sums
+    left = train - n_b
+    while left > 0:
+        m = min(65536, left)
+        sur.append_eval(eng, _draws(rng, center, chol_r, m, 1.5), k=k)
+        left -= m
+    t_data = time.perf_counter() - t0
+    log(f"training set: {train} points in {t_data:.2f} s (base fit {t_base_fit:.2f} s)")
+
+    # 3. training
+    t0 = time.perf_counter()
+    hist = sur.train(epochs=epochs, lr=lr, batch=min(batch, train - train % 8))
     t_train = time.perf_counter() - t0
-    sur.attach(wl.data, ratio, llh_type)
+    log(f"training: {epochs} epochs, {t_train:.2f} s, loss {hist[0]:.4g} -> {hist[-1]:.4g}")
 
-    def f_sur(th):
-        return sur.stat_llh(th) + penalty(wl, icov, th)
+    def make_f_sur(su):
+        return lambda th: su.stat_llh(th) + penalty(wl.prior_mean, icov, th)
 
-    # surrogate error (sd of the differences between points) on held-out
-    # prior draws and on held-out pilot-chain states
-    def err_sd(pts):
-        ex = f_exact(pts)
-        sx = f_sur(pts)
-        return float(np.std((ex - ex.mean()) - (sx - sx.mean())))
-    sur_err_prior = err_sd(wl.draw_points(256, seed + 99))
-    sur_err_post = err_sd(pil[np.random.default_rng(seed + 98).choice(pil.shape[0], 256, replace=False)])
+    f_sur = make_f_sur(sur)
+    sur.set_chain(L, wl.prior_mean, icov)
+    lin = None
+    if linear:
+        lin = sur.linear_twin()
+        lin.attach(wl.data, None, llh_type)
+        lin.set_chain(L, wl.prior_mean, icov)
 
+    # surrogate error: sd of the differences between points at posterior
+    # states, and of the change over n_sub-step random-walk excursions
+    hrng = np.random.default_rng(seed + 99)
+    if post_samples is not None:
+        test = post_samples[hrng.choice(post_samples.shape[0], 256, replace=False)]
+    else:
+        test = _draws(hrng, center, chol_r, 256)
+    excur = test + (hrng.standard_normal((256, n_sub, P)) @ L.T).sum(axis=1)
+    f_t, f_e = f_exact(test), f_exact(excur)
+
+    def errs(su):
+        fs = make_f_sur(su)
+        e1 = fs(test) - f_t
+        e2 = fs(excur) - f_e
+        return {"posterior": float(np.std(e1 - e1.mean())), "excursion_difference": float(np.std(e2 - e1))}
+    err = {"with_network": errs(sur)}
+    if lin:
+        err["base_only"] = errs(lin)
+    err["exact_excursion_spread"] = float(np.std(f_e - f_t))
+    t0 = time.perf_counter()
+    for r in range(5):
+        sur.substeps(th0, None, n_sub, r)
+    t_sub = (time.perf_counter() - t0) / 5
+    t0 = time.perf_counter()
+    for _ in range(5):
+        f_exact(th0)
+    t_exact = (time.perf_counter() - t0) / 5
+
+    # 4. sampling, both samplers from the same states with the same proposal
+    def stage1_of(su):
+        return lambda th, fs, ns, sd: su.substeps(th, fs, ns, sd)
     p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7)
-    d = mcmc.delayed(f_exact, f_sur, th0, steps, L, n_sub=n_sub, seed=seed + 8)
-    b = steps // 5
-    ess_p = mcmc.ess(p["chains"], burn=b)
-    ess_d = mcmc.ess(d["chains"], burn=b)
-    xp = p["chains"][b:].reshape(-1, wl.n_params)
-    xd = d["chains"][b:].reshape(-1, wl.n_params)
-    sig = xp.std(0)
+    d = mcmc.delayed(f_exact, f_sur, th0, da_steps, L, n_sub=n_sub, seed=seed + 8, max_error=max_error,
+                     stage1=stage1_of(sur))
+    dl = mcmc.delayed(f_exact, None, th0, da_steps, L, n_sub=n_sub, seed=seed + 9, max_error=max_error,
+                      stage1=stage1_of(lin)) if lin else None
+    ess_p, st_p = _sampler_stats(p["chains"], p["seconds"], 0)
+    ess_d, st_d = _sampler_stats(d["chains"], d["seconds"], 0)
+    xp = p["chains"].reshape(-1, P)
+    xd = d["chains"].reshape(-1, P)
+    sig_p, sig_d = xp.std(0), xd.std(0)
+    mean_diff = np.abs(xd.mean(0) - xp.mean(0))
+    se = np.sqrt(sig_p ** 2 / ess_p + sig_d ** 2 / ess_d)
     res = {
-        "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
-        "train_points": train, "epochs": epochs, "train_seconds": t_train, "data_seconds": t_data,
-        "train_mse_first_last": [hist[0], hist[-1]],
-        "training_region": region, "pilot_steps": pilot_steps, "pilot_seconds": t_pilot,
-        "surrogate_llh_error_sd_prior_draws": sur_err_prior,
-        "surrogate_llh_error_sd_posterior": sur_err_post,
-        "chains": chains, "steps": steps, "n_sub": n_sub,
-        "plain": {"seconds": p["seconds"], "accept": p["accept"], "n_exact": p["n_exact"],
-                  "ess_min": float(ess_p.min()), "ess_median": float(np.median(ess_p)),
-                  "ess_per_s_min": float(ess_p.min() / p["seconds"]),
-                  "ess_per_s_median": float(np.median(ess_p) / p["seconds"])},
-        "delayed": {"seconds": d["seconds"], "stage2_accept": d["stage2_accept"], "accept": d["accept"],
-                    "n_exact": d["n_exact"], "n_surrogate": d["n_surrogate"],
-                    "fell_back_at_step": d["fell_back_at_step"],
-                    "stage2_llh_error_mean": d["surrogate_error_mean"],
-                    "ess_min": float(ess_d.min()), "ess_median": float(np.median(ess_d)),
-                    "ess_per_s_min": float(ess_d.min() / d["seconds"]),
-                    "ess_per_s_median": float(np.median(ess_d) / d["seconds"])},
-        "posterior_mean_diff_over_sigma_max": float(np.max(np.abs(xp.mean(0) - xd.mean(0)) / sig)),
-        "posterior_width_ratio_range": [float(np.min(xd.std(0) / sig)), float(np.max(xd.std(0) / sig))],
-        "total_seconds": time.perf_counter() - t_all,
+        "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {B} bins, {P} params",
+        "precision": precision, "chains": chains, "plain_steps": steps, "delayed_steps": da_steps, "n_sub": n_sub,
+        "fit": {"f": fr["f"], "iterations": fr["iterations"], "seconds": fr["seconds"]},
+        "pilot": {"proposal": proposal, "seconds": t_adapt, "scale": scale,
+                  "accept": ad["accept"] if proposal == "adapted" else None,
+                  "posterior_sd_median": float(np.median(np.sqrt(np.diag(cov_post))))},
+        "training": {"region": region, "points": train, "epochs": epochs, "base": f"additive, {nodes} nodes",
+                     "base_points": n_b, "base_data_seconds": t_base_data, "base_fit_seconds": t_base_fit,
+                     "data_seconds": t_data, "train_seconds": t_train, "loss_first_last": [hist[0], hist[-1]]},
+        "surrogate_llh_error_sd": err,
+        "seconds_per_step": {"surrogate_substeps": t_sub, "exact": t_exact, "points": chains},
+        "plain": dict(st_p, accept=p["accept"], n_exact=p["n_exact"]),
+        "delayed": dict(st_d, stage2_accept=d["stage2_accept"], accept=d["accept"], n_exact=d["n_exact"],
+                        n_surrogate=d["n_surrogate"], fell_back_at_step=d["fell_back_at_step"],
+                        stage2_llh_error_mean=d["surrogate_error_mean"]),
+        "posterior": {
+            "mean_diff_over_sigma_max": float((mean_diff / sig_p).max()),
+            "mean_diff_over_sigma_median": float(np.median(mean_diff / sig_p)),
+            "mean_diff_over_mc_se_max": float((mean_diff / se).max()),
+            "mean_diff_over_mc_se_rms": float(np.sqrt(np.mean((mean_diff / se) ** 2))),
+            "width_ratio_range": [float((sig_d / sig_p).min()), float((sig_d / sig_p).max())],
+            "width_ratio_median": float(np.median(sig_d / sig_p)),
+        },
+        "ess_per_s_gain_min": st_d["ess_per_s_min"] / st_p["ess_per_s_min"],
+        "ess_per_s_gain_median": st_d["ess_per_s_median"] / st_p["ess_per_s_median"],
     }
-    res["ess_per_s_gain_min"] = res["delayed"]["ess_per_s_min"] / max(res["plain"]["ess_per_s_min"], 1e-300)
-    res["ess_per_s_gain_median"] = res["delayed"]["ess_per_s_median"] / max(res["plain"]["ess_per_s_median"], 1e-300)
+    if dl is not None:
+        _, st_l = _sampler_stats(dl["chains"], dl["seconds"], 0)
+        res["delayed_base_only"] = dict(st_l, stage2_accept=dl["stage2_accept"],
+                                        fell_back_at_step=dl["fell_back_at_step"],
+                                        stage2_llh_error_mean=dl["surrogate_error_mean"])
+        res["network_gain_ess_per_s_median"] = st_d["ess_per_s_median"] / st_l["ess_per_s_median"]
+        lin.close()
+    res["total_seconds"] = time.perf_counter() - t_all
     sur.close()
     eng.close()
     return res
@@ -137,17 +240,24 @@ def run(events=0, train=16384, epochs=20, chains=64, steps=400, n_sub=10, seed=2
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--events", type=int, default=0)
-    ap.add_argument("--train", type=int, default=16384)
+    ap.add_argument("--train", type=int, default=65536)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--chains", type=int, default=64)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--da-steps", type=int, default=0)
     ap.add_argument("--n-sub", type=int, default=10)
+    ap.add_argument("--nodes", type=int, default=8)
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--region", default="pilot", choices=["pilot", "prior"])
-    ap.add_argument("--pilot-steps", type=int, default=200)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--region", default="posterior", choices=["posterior", "prior"])
+    ap.add_argument("--proposal", default="adapted", choices=["adapted", "prior"])
+    ap.add_argument("--no-linear", action="store_true")
+    ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args()
+    lg = (lambda m: print(m, file=sys.stderr, flush=True)) if a.verbose else None
     print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config,
-                         region=a.region, pilot_steps=a.pilot_steps)))
+                         precision=a.precision, region=a.region, proposal=a.proposal, nodes=a.nodes,
+                         linear=not a.no_linear, log=lg, da_steps=a.da_steps or None)))
 
 
 if __name__ == "__main__":

@@ -61,12 +61,43 @@ def plain(f_exact, theta0, n_steps, L, seed=0, record=True):
     return {"chains": out, "accept": acc / (n_steps * C), "n_exact": n_exact, "seconds": dt}
 
 
-def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True):
+def adapt(f_exact, theta0, cov0, cycles=4, steps=150, seed=0, target=0.234, record_last=True):
+    """Adaptive pilot of the plain sampler, as SimpleMcmc's adaptive proposal
+    (covarianceWindow / adaptiveCovTrials, SimpleMcmc.cpp:136-245): cycles of
+    ``steps`` random-walk steps; after each cycle the proposal covariance
+    becomes the covariance of the second half of the cycle's states pooled
+    over all chains, and its scale (starting at 2.38^2/P) moves towards the
+    target acceptance.  Returns the final states, the covariance, the scale
+    and the acceptance per cycle (and the last cycle's states)."""
+    th = np.array(theta0, dtype=np.float64)
+    C, P = th.shape
+    cov = np.array(cov0, dtype=np.float64)
+    scale = 2.38 ** 2 / P
+    acc = []
+    last = None
+    for c in range(cycles):
+        L = np.linalg.cholesky(scale * cov + 1e-12 * np.eye(P))
+        r = plain(f_exact, th, steps, L, seed=seed + 1000 * c)
+        th = r["chains"][-1].copy()
+        x = r["chains"][steps // 2:].reshape(-1, P)
+        cov = np.cov(x.T) + 1e-12 * np.eye(P)
+        acc.append(r["accept"])
+        scale *= float(np.exp(2.0 * (r["accept"] - target)))
+        last = r["chains"]
+    return {"theta": th, "cov": cov, "scale": scale, "accept": acc,
+            "chains": last if record_last else None}
+
+
+def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True, stage1=None):
+    """stage1: optional callable (theta, fs, n_sub, seed) -> (phi, fphi, n_acc)
+    that runs the surrogate sub-chains elsewhere (on the device, with the
+    same proposal L and its own random numbers); fs None asks for the
+    surrogate values at theta.  Without it the sub-chains run here on f_sur."""
     rng = np.random.default_rng(seed)
     th = np.array(theta0, dtype=np.float64)
     C, P = th.shape
     f = f_exact(th)
-    fs = f_sur(th)
+    fs = stage1(th, None, 0, seed)[1] if stage1 else f_sur(th)
     out = np.empty((n_steps, C, P)) if record else None
     stage1_moves = stage2_tries = stage2_acc = 0
     n_exact = C
@@ -89,15 +120,19 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
                 out[s] = th
             continue
         # stage 1: surrogate sub-chain of n_sub random-walk Metropolis steps
-        phi = th.copy()
-        fphi = fs.copy()
-        for _ in range(n_sub):
-            prop = phi + rng.standard_normal((C, P)) @ L.T
-            fprop = f_sur(prop)
-            n_sur += C
-            a = _mh_accept(rng, fprop, fphi)
-            phi[a] = prop[a]
-            fphi[a] = fprop[a]
+        if stage1:
+            phi, fphi, _ = stage1(th, fs, n_sub, seed * 1000003 + s + 1)
+            n_sur += C * n_sub
+        else:
+            phi = th.copy()
+            fphi = fs.copy()
+            for _ in range(n_sub):
+                prop = phi + rng.standard_normal((C, P)) @ L.T
+                fprop = f_sur(prop)
+                n_sur += C
+                a = _mh_accept(rng, fprop, fphi)
+                phi[a] = prop[a]
+                fphi[a] = fprop[a]
         moved = np.any(phi != th, axis=1)
         stage1_moves += int(moved.sum())
         if moved.any():
@@ -136,38 +171,37 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
     }
 
 
-def _autocorr(x):
-    n = x.shape[0]
-    x = x - x.mean(axis=0)
-    m = 1 << int(np.ceil(np.log2(2 * n)))
-    fx = np.fft.rfft(x, m, axis=0)
-    ac = np.fft.irfft(fx * np.conj(fx), m, axis=0)[:n]
-    v = ac[0]
-    v = np.where(v > 0, v, 1.0)
-    return ac / v
-
-
 def ess(chains, burn=0):
-    """Effective sample size per parameter, summed over chains, with Geyer's
-    initial positive (monotone) sequence estimator of the autocorrelation
-    time.  chains: [steps x chains x params]."""
-    x = chains[burn:]
+    """Effective sample size per parameter of a set of chains [steps x chains
+    x params]: the multi-chain estimator of Vehtari, Gelman, Simpson,
+    Carpenter & Buerkner (2021, without rank normalisation or splitting).
+    Lag-t autocorrelation from the within-chain autocovariances and the
+    between-chain variance, rho_t = 1 - (W - mean_c acov_c(t)) / var+, summed
+    with Geyer's initial positive (monotone) sequence.  Chains that have not
+    mixed (their means disagree) raise var+ and lower the ESS."""
+    x = np.asarray(chains[burn:], dtype=np.float64)
     n, C, P = x.shape
-    total = np.zeros(P)
+    if n < 4:
+        return np.full(P, float(n * C))
+    mc = x.mean(axis=0)  # [C x P]
+    m = 1 << int(np.ceil(np.log2(2 * n)))
+    acov = np.zeros((n, P))
     for c in range(C):
-        rho = _autocorr(x[:, c, :])  # [n x P]
-        tau = np.ones(P)
-        for p in range(P):
-            r = rho[:, p]
-            g_prev = np.inf
-            s = 0.0
-            for m in range(0, (n - 1) // 2):
-                g = r[2 * m] + r[2 * m + 1]
-                if g <= 0:
-                    break
-                g = min(g, g_prev)
-                s += g
-                g_prev = g
-            tau[p] = max(1.0, -1.0 + 2.0 * s)
-        total += n / tau
-    return total
+        y = x[:, c, :] - mc[c]
+        fy = np.fft.rfft(y, m, axis=0)
+        acov += np.fft.irfft(fy * np.conj(fy), m, axis=0)[:n] / n
+    acov /= C
+    W = acov[0] * n / (n - 1)
+    Bn = mc.var(axis=0, ddof=1) if C > 1 else np.zeros(P)
+    var_plus = (n - 1) / n * W + Bn
+    var_plus = np.where(var_plus > 0, var_plus, 1.0)
+    rho = 1.0 - (W - acov) / var_plus
+    M = (n - 1) // 2
+    gam = rho[0:2 * M:2] + rho[1:2 * M:2]
+    pos = gam > 0
+    stop = np.where(pos.all(axis=0), M, np.argmin(pos, axis=0))
+    mono = np.minimum.accumulate(np.where(pos, gam, 0.0), axis=0)
+    keep = np.arange(M)[:, None] < stop[None, :]
+    tau = -1.0 + 2.0 * np.where(keep, mono, 0.0).sum(axis=0)
+    tau = np.maximum(tau, 1.0 / np.log10(max(n * C, 10)))
+    return n * C / tau

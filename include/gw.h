@@ -313,9 +313,49 @@ int gwm_gradients(gwm_net* net, const float* x, const float* t, int32_t B, float
 int gwm_set_head(gwm_net* net, const float* in_mean, const float* in_scale, const float* base_w,
                  const float* base_b, const float* out_mu, const float* out_sd, const float* ratio,
                  const double* data);
+/* Additive head: predicted log rate = base_b + sum_k interp_k(x_k) + out_mu +
+ * out_sd * net(x), x = (theta - in_mean) / in_scale, with interp_k linear
+ * between `nodes` (>= 2) equally spaced values base_tab[k][0..nodes-1][bin]
+ * ([dims[0] x nodes x dims[n]], FP32) over x_k in [-lim, lim] and constant
+ * outside; Sum w^2 = exp(ratio_b + ratio_w x) * rate (ratio_w [dims[n] x
+ * dims[0]] optional, ratio_b [dims[n]] the log of the ratio). */
+int gwm_set_head_additive(gwm_net* net, const float* in_mean, const float* in_scale, int32_t nodes, float lim,
+                          const float* base_tab, const float* base_b, const float* out_mu, const float* out_sd,
+                          const float* ratio_w, const float* ratio_b, const double* data);
 /* Surrogate statistical likelihood (GW_LLH_*) of B points theta [B x dims[0]]
  * (host FP64) -> llh [B] (host); log_rates [B x dims[n]] optional. */
 int gwm_predict(gwm_net* net, const double* theta, int32_t B, int32_t llh_type, double* llh, double* log_rates);
+/* Training set held on the device: room for n_max points (clears the set). */
+int gwm_train_reserve(gwm_net* net, int64_t n_max);
+int gwm_train_size(gwm_net* net, int64_t* count);
+/* Appends K <= batch_max points theta [K x dims[0]] (host FP64) and their bin
+ * sums [K x dims[n]] (FP64; device memory when sums_on_device != 0).  The
+ * target is the standardised residual of log(sums) after the head's affine
+ * base, so gwm_set_head comes first. */
+int gwm_train_append(gwm_net* net, const double* theta, const double* sums, int32_t K, int32_t sums_on_device);
+/* As gwm_train_append, with the sums computed by the exact engine on the
+ * device (gw_eval_device on the network's stream); K <= the engine's k_max. */
+int gwm_train_append_eval(gwm_net* net, gw_engine* e, const double* theta, int32_t K);
+/* Rows [first, first + count) of the set to the host: x [count x dims[0]]
+ * standardised inputs, t [count x dims[n]] targets (either may be null). */
+int gwm_train_read(gwm_net* net, int64_t first, int32_t count, float* x, float* t);
+/* epochs x floor(size / batch) Adam steps over seeded per-epoch permutations
+ * of the device-resident set, learning rate cosine-decayed lr0 -> lr_min;
+ * losses [epochs] (optional) = mean loss per epoch. */
+int gwm_train_epochs(gwm_net* net, int32_t epochs, int32_t batch, float lr0, float lr_min, uint64_t seed,
+                     float* losses);
+/* Stage 1 of the delayed-acceptance sampler on the device: random-walk
+ * Metropolis sub-chains on f_s = surrogate statistical LLH + prior penalty
+ * (GUNDAM's -2 log L convention; accept when log u < -(f' - f) / 2).
+ * gwm_set_chain: proposal Cholesky factor L [P x P] (lower, row-major) and the
+ * Gaussian prior (mean [P], inverse covariance [P x P]; both null: none),
+ * P = dims[0].  gwm_substeps: n_sub steps for C <= batch_max chains from
+ * theta0 [C x P] with values f0 [C] (null: evaluated first); writes the end
+ * points phi [C x P], fphi [C] and the accepted sub-steps n_acc [C] (optional).
+ * Normals and uniforms come from a counter-based hash of (seed, step, chain). */
+int gwm_set_chain(gwm_net* net, const double* prop_chol, const double* prior_mean, const double* prior_icov);
+int gwm_substeps(gwm_net* net, const double* theta0, const double* f0, int32_t C, int32_t n_sub, int32_t llh_type,
+                 uint64_t seed, double* phi, double* fphi, int32_t* n_acc);
 /* The tensor-core GEMM alone: C [M x N] = A [M x K] * B [N x K]^T, BF16 in (raw bits), FP32 out, host arrays. */
 int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, int32_t N, int32_t K, float* C);
 

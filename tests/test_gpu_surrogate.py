@@ -127,3 +127,184 @@ def test_training_lowers_loss_and_beats_affine_base():
     lin = np.mean((s.log_rates_linear(te) - truth(te)) ** 2)
     assert full < 0.5 * lin
     s.close()
+
+
+def test_device_training_set_and_loop():
+    """Targets formed on the device (engine -> log sums -> affine residual)
+    equal the FP64 host formula, the host-sums and engine paths agree, the
+    native Adam loop lowers the loss, and the trained surrogate's likelihood
+    error is below that of the affine base alone."""
+    from gundam_gb300.engine import Engine
+    from gundam_gb300.workload import Workload
+    import gundam_gb300._native as Nn
+    wl = Workload("c2", n_events=200000, seed=4)
+    eng = Engine.from_workload(wl, precision="fp32", k_max=64, llh_type=Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    rng = np.random.default_rng(5)
+    chol = np.linalg.cholesky(wl.prior_cov)
+    # wide enough that the response is visibly non-linear
+    th = rng.standard_normal((1024, wl.n_params)) @ chol.T * 0.4
+    sums = np.empty((th.shape[0], wl.n_bins))
+    sums2 = np.empty_like(sums)
+    for s0 in range(0, th.shape[0], 64):
+        a, b, _, _ = eng.eval(th[s0:s0 + 64])
+        sums[s0:s0 + 64], sums2[s0:s0 + 64] = a, b
+    logs = np.log(np.maximum(sums, 1e-300))
+    sur = Surrogate(wl.n_params, wl.n_bins, hidden=(128, 128), batch_max=512, seed=3)
+    sur.fit_affine(th[:512], logs[:512])
+    ratio = np.where(sums[:512] > 0, sums2[:512] / np.maximum(sums[:512], 1e-300), 1.0).mean(axis=0)
+    # data consistent with this small sample (no counts in bins it leaves empty)
+    data = np.round(sums.mean(axis=0))
+    eng.set_data(data)
+    sur.attach(data, ratio, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    sur.reserve(1024 + 64)
+    sur.append(th[:512], sums[:512])
+    sur.append_eval(eng, th[512:], k=64)
+    sur.append_eval(eng, th[:64], k=64)
+    assert sur.size() == 1088
+    x, t = sur.read(0, 1088)
+    z = (th - sur.mu) / sur.sd
+    ref = (logs - (np.hstack([np.ones((z.shape[0], 1)), z]) @ sur.A) - sur.r_mu) / sur.r_sd
+    assert np.abs(x[:1024] - z).max() < 1e-5 * max(1.0, np.abs(z).max())
+    scale = np.abs(logs).max() / sur.r_sd.min()
+    assert np.abs(t[:1024] - ref).max() < 2e-6 * scale
+    assert np.array_equal(t[1024:], t[:64])  # engine path == host-sums path, bit for bit
+    hist = sur.train(epochs=150, lr=2e-3, batch=256)
+    assert hist[-1] < 0.6 * hist[0], hist
+    lin = sur.linear_twin()
+    lin.attach(data, ratio, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    te = rng.standard_normal((256, wl.n_params)) @ chol.T * 0.4
+    ex = np.concatenate([eng.eval(te[i:i + 64])[3] for i in range(0, 256, 64)])
+    def err(s):
+        d = s.stat_llh(te) - ex
+        return np.std(d - d.mean())
+    e_sur, e_lin = err(sur), err(lin)
+    assert e_sur < e_lin, (e_sur, e_lin)
+    lin.close()
+    sur.close()
+    eng.close()
+
+
+M64 = (1 << 64) - 1
+
+
+def _mix64(z):
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def _hash4(seed, step, chain, k):
+    h = _mix64((seed + 0x9E3779B97F4A7C15) & M64)
+    h = _mix64(h ^ ((step * 0xD1B54A32D192ED03) & M64))
+    h = _mix64(h ^ ((chain * 0xABC98388FB8FAC03) & M64))
+    return _mix64(h ^ ((k * 0x8CB92BA72F3D8DD7) & M64))
+
+
+def _u01(h):
+    return ((h >> 11) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def _normals(seed, step, chain, P):
+    n = np.empty(P)
+    for k2 in range((P + 1) // 2):
+        r = np.sqrt(-2.0 * np.log(_u01(_hash4(seed, step, chain, 2 * k2))))
+        a = 2.0 * np.pi * _u01(_hash4(seed, step, chain, 2 * k2 + 1))
+        n[2 * k2] = r * np.cos(a)
+        if 2 * k2 + 1 < P:
+            n[2 * k2 + 1] = r * np.sin(a)
+    return n
+
+
+@pytest.fixture(scope="module")
+def c2_small():
+    from gundam_gb300.engine import Engine
+    from gundam_gb300.workload import Workload
+    import gundam_gb300._native as Nn
+    wl = Workload("c2", n_events=200000, seed=4)
+    eng = Engine.from_workload(wl, precision="fp32", k_max=64, llh_type=Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    rng = np.random.default_rng(6)
+    chol = np.linalg.cholesky(wl.prior_cov)
+    th = rng.standard_normal((1024, wl.n_params)) @ chol.T * 0.1
+    sums = np.empty((th.shape[0], wl.n_bins))
+    sums2 = np.empty_like(sums)
+    for s0 in range(0, th.shape[0], 64):
+        a, b, _, _ = eng.eval(th[s0:s0 + 64])
+        sums[s0:s0 + 64], sums2[s0:s0 + 64] = a, b
+    sur = Surrogate(wl.n_params, wl.n_bins, hidden=(128, 128), batch_max=512, seed=3)
+    ok = sums > 0  # this small workload has empty bins
+    logs = np.log(np.where(ok, sums, 1e-300))
+    lratio = np.where(ok, np.log(np.where(ok, sums2, 1.0)) - np.log(np.where(ok, sums, 1.0)), 0.0)
+    sur.fit_additive(th, logs, log_ratio=lratio, nodes=6)
+    # data consistent with this small sample (no counts in bins it leaves empty)
+    data = np.round(sums.mean(axis=0))
+    sur.attach(data, None, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    sur.test_data = data
+    yield wl, eng, sur, th, sums
+    sur.close()
+    eng.close()
+
+
+def test_additive_head_matches_host(c2_small):
+    """Device head (FP32 additive base + network) against the FP64 host
+    formula; device LLH against the oracle's per-bin likelihood of the same
+    rates and modelled sum of w^2; device targets against the host residual."""
+    from oracle.oracle import llh_bin
+    import gundam_gb300._native as Nn
+    wl, eng, sur, th, sums = c2_small
+    pts = th[:16]
+    llh, lr = sur.device_log_rates(pts)
+    host = sur.log_rates(pts)
+    live = (sums > 0).all(axis=0)
+    assert np.abs(lr - host)[:, live].max() < 2e-5 * max(1.0, np.abs(host[:, live]).max())
+    z = (pts - sur.mu) / sur.sd
+    lratio = sur.rb[None, :] + z @ sur.rw.T
+    for m in range(4):
+        mu = np.exp(lr[m])
+        s2 = np.exp(lr[m] + lratio[m])
+        ref = sum(llh_bin(Nn.GW_LLH_BARLOW_BEESTON_OA2021, sur.test_data[b], mu[b], np.sqrt(s2[b]))
+                  for b in range(wl.n_bins))
+        # stage-1 terms are FP32 per bin (summed in FP64): ~1e-5 per bin
+        assert abs(llh[m] - ref) < 1e-6 * max(1.0, abs(ref)) + 2e-2
+    sur.reserve(64)
+    sur.append(th[:64], sums[:64])
+    _, t = sur.read(0, 64)
+    ls = np.log(np.maximum(sums, 1e-300))
+    ref_t = (ls[:64] - sur.base(th[:64]) - sur.r_mu) / sur.r_sd
+    live = (sums > 0).all(axis=0)
+    scale = np.abs(ls[:, live]).max() / sur.r_sd[live].min()
+    t, ref_t = t[:, live], ref_t[:, live]
+    assert np.abs(t - ref_t).max() < 2e-6 * scale
+
+
+def test_device_subchain_matches_host_replica(c2_small):
+    """The device sub-chain takes the same steps as a host replica fed with
+    the same counter-based random numbers and the device surrogate values."""
+    wl, eng, sur, th, sums = c2_small
+    P = wl.n_params
+    icov = wl.prior_icov
+    L = np.linalg.cholesky(0.02 * 2.38 ** 2 / P * wl.prior_cov)
+    sur.set_chain(L, wl.prior_mean, icov)
+    C, n_sub, seed = 8, 4, 12345
+    th0 = th[100:100 + C].copy()
+
+    def f(x):
+        d = np.atleast_2d(x) - wl.prior_mean
+        return sur.stat_llh(x) + np.sum((d @ icov) * d, axis=1)
+    _, f_init, _ = sur.substeps(th0, None, 0, seed)
+    # the device penalty is FP32 (the host one FP64)
+    assert np.allclose(f_init, f(th0), rtol=1e-6, atol=1e-4)
+    phi, fphi, nacc = sur.substeps(th0, f_init, n_sub, seed)
+    phi2, fphi2, nacc2 = sur.substeps(th0, f_init, n_sub, seed)
+    assert np.array_equal(phi, phi2) and np.array_equal(fphi, fphi2) and np.array_equal(nacc, nacc2)
+    cur, fc, acc = th0.copy(), f_init.copy(), np.zeros(C, np.int64)
+    for st in range(1, n_sub + 1):
+        prop = np.stack([cur[c] + L @ _normals(seed, st, c, P) for c in range(C)])
+        fp = f(prop)
+        for c in range(C):
+            if np.log(_u01(_hash4(seed, st, c, 0xFFFFFFFF))) < -(fp[c] - fc[c]) / 2:
+                cur[c], fc[c], acc[c] = prop[c], fp[c], acc[c] + 1
+    assert np.array_equal(nacc, acc)
+    # increments are FP32 on the device
+    assert np.allclose(phi, cur, rtol=0, atol=1e-6)
+    assert np.allclose(fphi, fc, rtol=1e-6, atol=1e-4)
+    assert acc.sum() > 0
