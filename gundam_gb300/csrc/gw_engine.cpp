@@ -719,7 +719,9 @@ int build_and_upload(gw_engine* e) {
   }
 
   // 4. tiles
-  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : 24576) / (int64_t)tsz;
+  // default payload per tile: 23936 bytes, so that the K = 1 kernel's two
+  // stages (payload + headers + event data) keep three CTAs per SM
+  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : 23936) / (int64_t)tsz;
   cap_elems = std::min<int64_t>(cap_elems, kMaxPayloadElems);
   cap_elems = std::max<int64_t>(cap_elems, 64);
   std::vector<TilePlan> tiles;
@@ -902,6 +904,11 @@ int build_and_upload(gw_engine* e) {
   v.cap = e->cap;
   v.tile_payload_bytes = (int)(((cap_elems * tsz) + 127) & ~(int64_t)127);
 
+  // the K = 1 kernel copies a tile's headers, event info and base weights
+  // with bulk copies rounded out to 16-byte boundaries: pad each array
+  hdr.resize(hdr.size() + 2, 0);
+  evinfo.resize(evinfo.size() + 8, 0);
+  w0.resize(w0.size() + 4, T(0));
   if ((rc = upload(tdesc.data(), tdesc.size() * sizeof(TileDesc), &p))) return rc;
   v.tiles = (const TileDesc*)p;
   if ((rc = upload(hdr.data(), hdr.size() * sizeof(uint64_t), &p))) return rc;

@@ -85,17 +85,20 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
-// Shared-memory matrix descriptor, no swizzle: start address, byte offset
-// between core matrices adjacent along K (LBO) and along M/N (SBO).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+// Shared-memory matrix descriptor, K-major with the 128-byte swizzle: rows of
+// 64 BF16 (128 bytes), 8-row atoms of 1024 bytes (SBO) whose 16-byte chunks
+// are XOR-permuted by the row within the atom (the pattern the TMA unit
+// writes with CU_TENSOR_MAP_SWIZZLE_128B into 1024-byte-aligned buffers);
+// LBO is unused for this layout.  A K step of 16 elements adds 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version
+  d |= (uint64_t)1 << 16;             // LBO (unused)
+  d |= (uint64_t)(1024 >> 4) << 32;   // SBO
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // layout: 128-byte swizzle
   return d;
 }
 
@@ -118,15 +121,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + __expf(-z)); }
 
@@ -171,10 +165,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 
 // Pipelined GEMM tile, C[128 x BN] = A[128 x K] * B[BN x K]^T.
 //   * thread 0 (warp 0) issues the TMA loads of each 64-wide K tile into one
-//     of S shared-memory stages (8 boxes of 8 K-elements per operand, so each
-//     stage holds core matrices (8 rows x 16 bytes) with LBO = rows * 16 bytes
-//     between K-neighbours and SBO = 128 bytes between row-neighbours);
-//     rows beyond M / N and columns beyond K arrive as zeros;
+//     of S shared-memory stages (one box of 64 K-elements x rows per operand,
+//     128-byte swizzle, 1024-byte-aligned stages); rows beyond M / N and
+//     columns beyond K arrive as zeros;
 //   * thread 32 (warp 1) waits for a stage, issues its four K = 16 MMAs and
 //     commits them to the stage's "empty" barrier, which lets the producer
 //     refill it; a final commit signals the epilogue;
@@ -227,11 +220,8 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const __grid_constant__ CUten
       unsigned char* a = smem + st * kStage;
       unsigned char* b = a + kA;
       mbar_arrive_expect(&full[st], (uint32_t)kStage);
-#pragma unroll
-      for (int j = 0; j < kBK / 8; ++j) {
-        tma_load_2d(a + j * (kBM * 16), &tmA, kt * kBK + 8 * j, m0, &full[st]);
-        tma_load_2d(b + j * (BN * 16), &tmB, kt * kBK + 8 * j, n0, &full[st]);
-      }
+      tma_load_2d(a, &tmA, kt * kBK, m0, &full[st]);
+      tma_load_2d(b, &tmB, kt * kBK, n0, &full[st]);
       produced = kt + 1;
     }
   } else if (tid == 32) {
@@ -249,8 +239,8 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const __grid_constant__ CUten
       const uint32_t a0 = smem_u32(smem + st * kStage), b0 = a0 + kA;
 #pragma unroll
       for (int s16 = 0; s16 < kBK / 16; ++s16) {
-        const uint64_t ad = smem_desc(a0 + s16 * 2 * (kBM * 16), kBM * 16, 128);
-        const uint64_t bd = smem_desc(b0 + s16 * 2 * (BN * 16), BN * 16, 128);
+        const uint64_t ad = smem_desc_sw128(a0 + s16 * 32);
+        const uint64_t bd = smem_desc_sw128(b0 + s16 * 32);
         mma_bf16(tmem, ad, bd, idesc, (kt > 0 || s16 > 0) ? 1u : 0u);
       }
       mma_commit(&empty[st]);
@@ -490,12 +480,6 @@ __device__ __forceinline__ float head_base(const Head& h, const float* __restric
   return acc;
 }
 
-__device__ __forceinline__ double head_log_ratio(const Head& h, const float* __restrict__ x, int bin) {
-  float acc = h.r_b[bin];
-  if (h.r_w)
-    for (int k = 0; k < h.din; ++k) acc = fmaf(x[k], h.r_w[(size_t)k * h.nb + bin], acc);
-  return (double)acc;
-}
 
 // log(data / mc) for data, mc > 0: log1p((data - mc) / mc) near 1, where
 // log(data) - log(mc) would cancel in FP32, and the difference of logs away
@@ -745,17 +729,18 @@ static EncodeTiledFn encode_tiled() {
 }
 
 // Tensor map of a row-major BF16 matrix [rows x K] (K % 8 == 0, 16-byte
-// aligned rows) read in boxes of 8 K-elements x box_rows rows, zero fill.
+// aligned rows) read in boxes of 64 K-elements (128 bytes) x box_rows rows
+// with the 128-byte swizzle, zero fill.
 static int make_map(gwm_net* n, CUtensorMap* map, const bf16* p, int rows, int K, int box_rows) {
   EncodeTiledFn enc = encode_tiled();
   if (!enc) return gwm_fail(n, GW_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   if (((uintptr_t)p & 15) != 0) return gwm_fail(n, GW_ERR_ARG, "GEMM operand not 16-byte aligned");
   const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-  const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)gwm::kBK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)p, dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return gwm_fail(n, GW_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return GW_OK;
@@ -1180,7 +1165,7 @@ extern "C" int gwm_set_head_additive(gwm_net* n, const float* in_mean, const flo
 // Fused head + likelihood of the first C rows of the network's output (xin
 // holds their standardised inputs): h_llh [C]; with `outputs`, h_sums,
 // h_sums2 and h_logr too.
-static int head_llh(gwm_net* n, int C, int llh_type, bool outputs) {
+static int head_llh(gwm_net* n, int C, int llh_type, bool outputs, bool finish = true) {
   const int nb = n->dims[n->n_layers], L = n->n_layers;
   constexpr int kPPT = 2;
   const int nbx = (nb + 31) / 32;
@@ -1196,7 +1181,7 @@ static int head_llh(gwm_net* n, int C, int llh_type, bool outputs) {
   gwm::k_head_llh<kPPT><<<grid, dim3(32, 8), shm, n->stream>>>(
       head_view(n), n->xin, n->z[L - 1], C, n->h_data, llh_type, n->h_part, outputs ? n->h_sums : nullptr,
       outputs ? n->h_sums2 : nullptr, outputs ? n->h_logr : nullptr);
-  gwm::k_llh_finish<<<(C + 7) / 8, 256, 0, n->stream>>>(n->h_part, nbx, C, n->h_llh);
+  if (finish) gwm::k_llh_finish<<<(C + 7) / 8, 256, 0, n->stream>>>(n->h_part, nbx, C, n->h_llh);
   GWM_CUDA(n, cudaGetLastError());
   return GW_OK;
 }
@@ -1208,7 +1193,7 @@ extern "C" int gwm_predict(gwm_net* n, const double* theta, int32_t B, int32_t l
   if (!n || !theta || !llh || B < 1 || B > n->batch_max) return gwm_fail(n, GW_ERR_ARG, "gwm_predict: bad batch");
   if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_predict: gwm_set_head has not been called");
   GWM_CUDA(n, cudaSetDevice(n->device));
-  const int din = n->dims[0], nb = n->dims[n->n_layers], L = n->n_layers;
+  const int din = n->dims[0], nb = n->dims[n->n_layers];
   const int Bp = ((B + 7) / 8) * 8;  // GEMM rows in multiples of 8; the extra rows are zeros
   if (Bp > n->batch_max) return gwm_fail(n, GW_ERR_ARG, "gwm_predict: batch above batch_max after padding");
   if (Bp > B) GWM_CUDA(n, cudaMemsetAsync(n->h_theta, 0, sizeof(double) * (size_t)Bp * din, n->stream));
@@ -1429,22 +1414,26 @@ __device__ __forceinline__ uint64_t hash4(uint64_t seed, uint64_t step, uint64_t
 // uniform in (0, 1), 53 bits
 __device__ __forceinline__ double u01(uint64_t h) { return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
 
-// Block per chain: n[k] standard normals (Box-Muller on hash pairs, FP64),
-// then prop[c][p] = phi[c][p] + sum_{k<=p} L[p][k] n[k] with the increment in
-// FP32 (Lt = L transposed, so that thread p reads column p coalesced).  The
-// increment depends on n alone, so the proposal stays symmetric.
-__global__ void k_propose(const double* __restrict__ phi, int P, const float* __restrict__ Lt, uint64_t seed,
-                          uint64_t step, double* __restrict__ prop) {
+// First step of a sub-step, block per chain: standard normals n[k]
+// (Box-Muller on hash pairs, FP32), the proposal prop = phi + L n with the
+// increment in FP32 (Lt = L transposed, so that thread p reads column p
+// coalesced; the increment depends on n alone, so the proposal is
+// symmetric), written in FP64, and its standardised inputs
+// x = (prop - mean) / scale (FP32, as k_standardize) with the BF16 row of the
+// first GEMM (as k_rows_to_bf16).
+__global__ void k_propose_stage(const double* __restrict__ phi, int P, const float* __restrict__ Lt, uint64_t seed,
+                                uint64_t step, double* __restrict__ prop, const float* __restrict__ mean,
+                                const float* __restrict__ scale, float* __restrict__ x, bf16* __restrict__ h0) {
   extern __shared__ float nrm[];
   const int c = blockIdx.x;
   for (int k2 = threadIdx.x; 2 * k2 < P; k2 += blockDim.x) {
-    const double u1 = u01(hash4(seed, step, c, 2 * k2));
-    const double u2 = u01(hash4(seed, step, c, 2 * k2 + 1));
-    const double r = sqrt(-2.0 * log(u1));
-    double sn, cs;
-    sincospi(2.0 * u2, &sn, &cs);
-    nrm[2 * k2] = (float)(r * cs);
-    if (2 * k2 + 1 < P) nrm[2 * k2 + 1] = (float)(r * sn);
+    const float u1 = (float)u01(hash4(seed, step, c, 2 * k2));
+    const float u2 = (float)u01(hash4(seed, step, c, 2 * k2 + 1));
+    const float r = sqrtf(-2.f * logf(u1));
+    float sn, cs;
+    sincospif(2.f * u2, &sn, &cs);
+    nrm[2 * k2] = r * cs;
+    if (2 * k2 + 1 < P) nrm[2 * k2 + 1] = r * sn;
   }
   __syncthreads();
   for (int p = threadIdx.x; p < P; p += blockDim.x) {
@@ -1457,69 +1446,79 @@ __global__ void k_propose(const double* __restrict__ phi, int P, const float* __
       a3 = fmaf(Lt[(size_t)(k + 3) * P + p], nrm[k + 3], a3);
     }
     for (; k <= p; ++k) a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
-    prop[(size_t)c * P + p] = phi[(size_t)c * P + p] + (double)((a0 + a1) + (a2 + a3));
+    const size_t o = (size_t)c * P + p;
+    const double v = phi[o] + (double)((a0 + a1) + (a2 + a3));
+    prop[o] = v;
+    const float z = (float)((v - (double)mean[p]) / (double)scale[p]);
+    x[o] = z;
+    h0[o] = __float2bfloat16(z);
   }
 }
 
-// Block per chain: pen[c] = d^T C^-1 d, d = x[c] - m, in FP32 (C^-1 symmetric,
-// read by columns), fixed-order reduction.
-__global__ void k_penalty(const double* __restrict__ x, int P, const double* __restrict__ m,
-                          const float* __restrict__ icov, double* __restrict__ pen) {
+// Last step of a sub-step, block per chain: the surrogate LLH of the proposal
+// from the per-block partials (the order of k_llh_finish), its prior penalty
+// d^T C^-1 d, d = prop - m (FP32, C^-1 read by columns, fixed-order
+// reduction; skipped when m is null), and the Metropolis decision on
+// f = llh + penalty: accept when log u < -(f - f_current) / 2 with u from the
+// hash of (seed, step, chain); NaN proposals are rejected.  first != 0 takes
+// the value unconditionally (the initial evaluation).
+__global__ void k_finish_accept(const double* __restrict__ part, int nblk, const double* __restrict__ prop, int P,
+                                const double* __restrict__ m, const float* __restrict__ icov, uint64_t seed,
+                                uint64_t step, int first, double* __restrict__ phi, double* __restrict__ f,
+                                int32_t* __restrict__ n_acc) {
   extern __shared__ float shf[];
   float* d = shf;          // [P]
-  float* part = shf + P;   // [blockDim.x]
-  const int c = blockIdx.x;
-  for (int p = threadIdx.x; p < P; p += blockDim.x) d[p] = (float)(x[(size_t)c * P + p] - m[p]);
-  __syncthreads();
-  float acc = 0.f;
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
-    int k = 0;
-    for (; k + 4 <= P; k += 4) {
-      u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
-      u1 = fmaf(icov[(size_t)(k + 1) * P + p], d[k + 1], u1);
-      u2 = fmaf(icov[(size_t)(k + 2) * P + p], d[k + 2], u2);
-      u3 = fmaf(icov[(size_t)(k + 3) * P + p], d[k + 3], u3);
+  float* red = shf + P;    // [blockDim.x]
+  __shared__ double s_llh;
+  __shared__ int s_take;
+  const int c = blockIdx.x, lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int b = lane; b < nblk; b += 32) t += part[(size_t)c * nblk + b];
+    for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0) s_llh = t;
+  }
+  double pen = 0.0;
+  if (m) {
+    for (int p = threadIdx.x; p < P; p += blockDim.x) d[p] = (float)(prop[(size_t)c * P + p] - m[p]);
+    __syncthreads();
+    float acc = 0.f;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+      float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
+      int k = 0;
+      for (; k + 4 <= P; k += 4) {
+        u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+        u1 = fmaf(icov[(size_t)(k + 1) * P + p], d[k + 1], u1);
+        u2 = fmaf(icov[(size_t)(k + 2) * P + p], d[k + 2], u2);
+        u3 = fmaf(icov[(size_t)(k + 3) * P + p], d[k + 3], u3);
+      }
+      for (; k < P; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+      acc = fmaf(d[p], (u0 + u1) + (u2 + u3), acc);
     }
-    for (; k < P; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
-    acc = fmaf(d[p], (u0 + u1) + (u2 + u3), acc);
+    red[threadIdx.x] = acc;
   }
-  part[threadIdx.x] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < (int)blockDim.x; ++i) s += (double)part[i];
-    pen[c] = s;
+    if (m)
+      for (int i = 0; i < (int)blockDim.x; ++i) pen += (double)red[i];
+    const double fn = s_llh + pen;
+    int take;
+    if (first) {
+      f[c] = fn;
+      take = 0;
+    } else {
+      const double u = u01(hash4(seed, step, c, 0xFFFFFFFFull));
+      take = log(u) < -(fn - f[c]) * 0.5;  // NaN proposals are rejected
+      if (take) {
+        f[c] = fn;
+        n_acc[c] += 1;
+      }
+    }
+    s_take = take;
   }
-}
-
-// Block per chain: Metropolis decision on f = llh + pen (pen optional); on
-// acceptance the proposal row replaces phi and f.  step == ~0 marks the
-// initial evaluation (f taken unconditionally).
-__global__ void k_accept(const double* __restrict__ prop, const double* __restrict__ llh,
-                         const double* __restrict__ pen, int P, uint64_t seed, uint64_t step, int first,
-                         double* __restrict__ phi, double* __restrict__ f, int32_t* __restrict__ n_acc) {
-  const int c = blockIdx.x;
-  const double fn = llh[c] + (pen ? pen[c] : 0.0);
-  bool take;
-  if (first) {
-    take = false;
-  } else {
-    const double u = u01(hash4(seed, step, c, 0xFFFFFFFFull));
-    const double d = -(fn - f[c]) * 0.5;
-    take = log(u) < d;  // NaN proposals are rejected
-  }
-  if (first) {
-    if (threadIdx.x == 0) f[c] = fn;
-    return;
-  }
-  if (!take) return;
-  for (int p = threadIdx.x; p < P; p += blockDim.x) phi[(size_t)c * P + p] = prop[(size_t)c * P + p];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    f[c] = fn;
-    n_acc[c] += 1;
-  }
+  if (s_take)
+    for (int p = threadIdx.x; p < P; p += blockDim.x) phi[(size_t)c * P + p] = prop[(size_t)c * P + p];
 }
 
 }  // namespace
@@ -1546,8 +1545,9 @@ static void chain_free(gwm_chain_state* s) {
   delete s;
 }
 
-// Evaluates the surrogate statistical LLH of the first C rows of h_theta
-// (device) into h_llh.  Rows C..roundup(C, 8) of h_theta must be finite.
+// Evaluates the surrogate of the first C rows of h_theta (device) up to the
+// per-block likelihood partials h_part.  Rows C..roundup(C, 8) of h_theta must
+// be finite.
 static int surrogate_llh_device(gwm_net* n, int C, int llh_type) {
   const int din = n->dims[0];
   const int Bp = ((C + 7) / 8) * 8;
@@ -1556,7 +1556,7 @@ static int surrogate_llh_device(gwm_net* n, int C, int llh_type) {
   int rc = stage_input(n, n->xin, nullptr, Bp, false);
   if (!rc) rc = forward(n, Bp);
   if (rc) return rc;
-  return head_llh(n, C, llh_type, false);
+  return head_llh(n, C, llh_type, false, false);
 }
 
 // Proposal Cholesky factor L [P x P] (lower, row-major, host FP64) and the
@@ -1621,13 +1621,14 @@ extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, 
   const unsigned thr = P >= 256 ? 256 : (unsigned)(((P + 31) / 32) * 32);
   const bool prior = s->prior;
   const size_t sh_prop = sizeof(float) * (size_t)(P + 1);
-  const size_t sh_pen = sizeof(float) * ((size_t)P + thr);
   GWM_CUDA(n, cudaMemcpyAsync(s->phi, theta0, sizeof(double) * (size_t)C * P, cudaMemcpyHostToDevice, n->stream));
   GWM_CUDA(n, cudaMemsetAsync(s->nacc, 0, sizeof(int32_t) * C, n->stream));
   // rows C..Bp of the staging buffer stay finite (zeros)
   if (Bp > C)
     GWM_CUDA(n, cudaMemsetAsync(n->h_theta + (size_t)C * P, 0, sizeof(double) * (size_t)(Bp - C) * P, n->stream));
   int rc = GW_OK;
+  const int nbx = (n->dims[n->n_layers] + 31) / 32;
+  const size_t sh_fin = sizeof(float) * ((size_t)P + thr);
   if (f0) {
     GWM_CUDA(n, cudaMemcpyAsync(s->f, f0, sizeof(double) * C, cudaMemcpyHostToDevice, n->stream));
   } else {
@@ -1635,25 +1636,21 @@ extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, 
                                 n->stream));
     rc = surrogate_llh_device(n, C, llh_type);
     if (rc) return rc;
-    if (prior) {
-      gwm::k_penalty<<<C, thr, sh_pen, n->stream>>>(s->phi, P, s->m, s->icov, s->pen);
-      GWM_CUDA(n, cudaGetLastError());
-    }
-    gwm::k_accept<<<C, thr, 0, n->stream>>>(s->phi, n->h_llh, prior ? s->pen : nullptr, P, seed, 0, 1, s->phi, s->f,
-                                          s->nacc);
+    gwm::k_finish_accept<<<C, thr, sh_fin, n->stream>>>(n->h_part, nbx, s->phi, P, prior ? s->m : nullptr, s->icov,
+                                                       seed, 0, 1, s->phi, s->f, s->nacc);
     GWM_CUDA(n, cudaGetLastError());
   }
+  // rows C..Bp of the first GEMM's input stay zero through the sub-steps
+  if (Bp > C) GWM_CUDA(n, cudaMemsetAsync(n->h[0] + (size_t)C * P, 0, sizeof(bf16) * (size_t)(Bp - C) * P, n->stream));
   for (int st = 0; st < n_sub && rc == GW_OK; ++st) {
-    gwm::k_propose<<<C, thr, sh_prop, n->stream>>>(s->phi, P, s->Lt, seed, (uint64_t)st + 1, n->h_theta);
+    gwm::k_propose_stage<<<C, thr, sh_prop, n->stream>>>(s->phi, P, s->Lt, seed, (uint64_t)st + 1, n->h_theta,
+                                                        n->h_mean, n->h_scale, n->xin, n->h[0]);
     GWM_CUDA(n, cudaGetLastError());
-    rc = surrogate_llh_device(n, C, llh_type);
+    rc = forward(n, Bp);
+    if (!rc) rc = head_llh(n, C, llh_type, false, false);
     if (rc) break;
-    if (prior) {
-      gwm::k_penalty<<<C, thr, sh_pen, n->stream>>>(n->h_theta, P, s->m, s->icov, s->pen);
-      GWM_CUDA(n, cudaGetLastError());
-    }
-    gwm::k_accept<<<C, thr, 0, n->stream>>>(n->h_theta, n->h_llh, prior ? s->pen : nullptr, P, seed,
-                                          (uint64_t)st + 1, 0, s->phi, s->f, s->nacc);
+    gwm::k_finish_accept<<<C, thr, sh_fin, n->stream>>>(n->h_part, nbx, n->h_theta, P, prior ? s->m : nullptr,
+                                                       s->icov, seed, (uint64_t)st + 1, 0, s->phi, s->f, s->nacc);
     GWM_CUDA(n, cudaGetLastError());
   }
   if (rc) return rc;

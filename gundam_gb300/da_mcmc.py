@@ -64,7 +64,8 @@ def _sampler_stats(ch, seconds, burn):
 
 def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=2, config="c2", log=None,
         precision="fp32", region="posterior", proposal="adapted", base_points=32768, nodes=8, batch=2048,
-        lr=1e-3, linear=True, max_error=20.0, adapt_cycles=6, adapt_steps=200, da_steps=None):
+        lr=1e-3, linear=True, max_error=20.0, adapt_cycles=6, adapt_steps=200, da_steps=None, thin=1,
+        warm_steps=500, burn_frac=0.1):
     """Fit, adapt, train, then sample with both samplers from the same states
     (``steps`` plain steps and ``da_steps`` (default: the same) delayed steps)."""
     log = log or (lambda *_: None)
@@ -185,21 +186,33 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
     # 4. sampling, both samplers from the same states with the same proposal
     def stage1_of(su):
         return lambda th, fs, ns, sd: su.substeps(th, fs, ns, sd)
-    p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7)
+    # both samplers start from the same states, taken after a delayed-
+    # acceptance warm-up (it mixes fastest) so that neither starts out of
+    # equilibrium; the first burn_frac of each run is discarded as well
+    t0 = time.perf_counter()
+    if warm_steps > 0:
+        w = mcmc.delayed(f_exact, f_sur, th0, warm_steps, L, n_sub=n_sub, seed=seed + 3, max_error=max_error,
+                         stage1=stage1_of(sur), record=False)
+        th0 = w["final"]
+    t_warm = time.perf_counter() - t0
+    p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7, thin=thin)
     d = mcmc.delayed(f_exact, f_sur, th0, da_steps, L, n_sub=n_sub, seed=seed + 8, max_error=max_error,
-                     stage1=stage1_of(sur))
+                     stage1=stage1_of(sur), thin=thin)
     dl = mcmc.delayed(f_exact, None, th0, da_steps, L, n_sub=n_sub, seed=seed + 9, max_error=max_error,
-                      stage1=stage1_of(lin)) if lin else None
-    ess_p, st_p = _sampler_stats(p["chains"], p["seconds"], 0)
-    ess_d, st_d = _sampler_stats(d["chains"], d["seconds"], 0)
-    xp = p["chains"].reshape(-1, P)
-    xd = d["chains"].reshape(-1, P)
+                      stage1=stage1_of(lin), thin=thin) if lin else None
+    bp = int(burn_frac * p["chains"].shape[0])
+    bd = int(burn_frac * d["chains"].shape[0])
+    ess_p, st_p = _sampler_stats(p["chains"], p["seconds"], bp)
+    ess_d, st_d = _sampler_stats(d["chains"], d["seconds"], bd)
+    xp = p["chains"][bp:].reshape(-1, P)
+    xd = d["chains"][bd:].reshape(-1, P)
     sig_p, sig_d = xp.std(0), xd.std(0)
     mean_diff = np.abs(xd.mean(0) - xp.mean(0))
     se = np.sqrt(sig_p ** 2 / ess_p + sig_d ** 2 / ess_d)
     res = {
         "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {B} bins, {P} params",
         "precision": precision, "chains": chains, "plain_steps": steps, "delayed_steps": da_steps, "n_sub": n_sub,
+        "thin": thin, "warm_steps": warm_steps, "warm_seconds": t_warm, "burn_fraction": burn_frac,
         "fit": {"f": fr["f"], "iterations": fr["iterations"], "seconds": fr["seconds"]},
         "pilot": {"proposal": proposal, "seconds": t_adapt, "scale": scale,
                   "accept": ad["accept"] if proposal == "adapted" else None,
@@ -225,7 +238,7 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
         "ess_per_s_gain_median": st_d["ess_per_s_median"] / st_p["ess_per_s_median"],
     }
     if dl is not None:
-        _, st_l = _sampler_stats(dl["chains"], dl["seconds"], 0)
+        _, st_l = _sampler_stats(dl["chains"], dl["seconds"], bd)
         res["delayed_base_only"] = dict(st_l, stage2_accept=dl["stage2_accept"],
                                         fell_back_at_step=dl["fell_back_at_step"],
                                         stage2_llh_error_mean=dl["surrogate_error_mean"])
@@ -251,13 +264,17 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--region", default="posterior", choices=["posterior", "prior"])
     ap.add_argument("--proposal", default="adapted", choices=["adapted", "prior"])
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--thin", type=int, default=1)
+    ap.add_argument("--warm-steps", type=int, default=500)
     ap.add_argument("--no-linear", action="store_true")
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args()
     lg = (lambda m: print(m, file=sys.stderr, flush=True)) if a.verbose else None
     print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config,
                          precision=a.precision, region=a.region, proposal=a.proposal, nodes=a.nodes,
-                         linear=not a.no_linear, log=lg, da_steps=a.da_steps or None)))
+                         linear=not a.no_linear, log=lg, da_steps=a.da_steps or None, lr=a.lr, thin=a.thin,
+                         warm_steps=a.warm_steps)))
 
 
 if __name__ == "__main__":

@@ -38,12 +38,13 @@ def _mh_accept(rng, f_new, f_old):
         return np.log(np.maximum(u, 1e-300)) < -(f_new - f_old) / 2.0
 
 
-def plain(f_exact, theta0, n_steps, L, seed=0, record=True):
+def plain(f_exact, theta0, n_steps, L, seed=0, record=True, thin=1):
+    """record: keep every ``thin``-th state ([n_steps // thin x chains x params])."""
     rng = np.random.default_rng(seed)
     th = np.array(theta0, dtype=np.float64)
     C, P = th.shape
     f = f_exact(th)
-    out = np.empty((n_steps, C, P)) if record else None
+    out = np.empty((n_steps // thin, C, P)) if record else None
     acc = 0
     n_exact = C
     t0 = time.perf_counter()
@@ -55,10 +56,10 @@ def plain(f_exact, theta0, n_steps, L, seed=0, record=True):
         th[a] = prop[a]
         f[a] = fp[a]
         acc += int(a.sum())
-        if record:
-            out[s] = th
+        if record and (s + 1) % thin == 0 and (s + 1) // thin <= out.shape[0]:
+            out[(s + 1) // thin - 1] = th
     dt = time.perf_counter() - t0
-    return {"chains": out, "accept": acc / (n_steps * C), "n_exact": n_exact, "seconds": dt}
+    return {"chains": out, "accept": acc / (n_steps * C), "n_exact": n_exact, "seconds": dt, "final": th}
 
 
 def adapt(f_exact, theta0, cov0, cycles=4, steps=150, seed=0, target=0.234, record_last=True):
@@ -88,7 +89,8 @@ def adapt(f_exact, theta0, cov0, cycles=4, steps=150, seed=0, target=0.234, reco
             "chains": last if record_last else None}
 
 
-def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True, stage1=None):
+def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True, stage1=None,
+            thin=1):
     """stage1: optional callable (theta, fs, n_sub, seed) -> (phi, fphi, n_acc)
     that runs the surrogate sub-chains elsewhere (on the device, with the
     same proposal L and its own random numbers); fs None asks for the
@@ -98,7 +100,11 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
     C, P = th.shape
     f = f_exact(th)
     fs = stage1(th, None, 0, seed)[1] if stage1 else f_sur(th)
-    out = np.empty((n_steps, C, P)) if record else None
+    out = np.empty((n_steps // thin, C, P)) if record else None
+
+    def keep(s):
+        if record and (s + 1) % thin == 0 and (s + 1) // thin <= out.shape[0]:
+            out[(s + 1) // thin - 1] = th
     stage1_moves = stage2_tries = stage2_acc = 0
     n_exact = C
     n_sur = C
@@ -116,8 +122,7 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
             fs[a] = np.nan
             stage2_tries += C
             stage2_acc += int(a.sum())
-            if record:
-                out[s] = th
+            keep(s)
             continue
         # stage 1: surrogate sub-chain of n_sub random-walk Metropolis steps
         if stage1:
@@ -155,8 +160,7 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
             recent = err_hist[-4 * C:]
             if len(recent) >= C and np.mean(recent) > max_error:
                 fell_back_at = s
-        if record:
-            out[s] = th
+        keep(s)
     dt = time.perf_counter() - t0
     return {
         "chains": out,
@@ -168,6 +172,7 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
         "seconds": dt,
         "surrogate_error_mean": float(np.mean(err_hist)) if err_hist else None,
         "fell_back_at_step": fell_back_at,
+        "final": th,
     }
 
 

