@@ -231,6 +231,44 @@ def time_device(eng, torch, d, K, steps, warmup, dist):
     return ms, kms / max(1, klaunch), launches
 
 
+def c3_sweep(local, steps=20, warmup=3):
+    """Batched reweighting of the 100k-event C1 workload: LLH evaluations/s at
+    K = 16, 64, 256 points per launch (FP32 dials, FP64 sums and LLH, the
+    launch chain captured in a CUDA graph, shape autotuned per K).  Device
+    parameters, CUDA events on the engine's stream."""
+    import torch
+
+    from gundam_gb300 import Engine, Workload
+
+    wl = Workload("c1", seed=2)
+    out = {"workload": f"c1: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
+           "note": "the C1 payload (~10 MB) is L2-resident"}
+    for K in (16, 64, 256):
+        eng = Engine.from_workload(wl, precision="fp32", k_max=K, llh_type=llh_type_for("c1"), device=local)
+        eng.autotune(K)
+        eng.use_graph(True)
+        pts = torch.from_numpy(wl.draw_points(K, 7)).cuda()
+        s = torch.empty((K, wl.n_bins), dtype=torch.float64, device="cuda")
+        s2 = torch.empty_like(s)
+        ll = torch.empty(K, dtype=torch.float64, device="cuda")
+        stream = torch.cuda.Stream()
+        sp = stream.cuda_stream
+        for _ in range(warmup):
+            eng.eval_device(pts.data_ptr(), K, s.data_ptr(), s2.data_ptr(), ll.data_ptr(), 0, sp)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            eng.eval_device(pts.data_ptr(), K, s.data_ptr(), s2.data_ptr(), ll.data_ptr(), 0, sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / steps
+        out[f"K{K}"] = {"evals_per_s": K * 1e3 / ms, "ms_per_launch": ms, "shape": list(eng.shape())}
+        eng.sync()
+        eng.close()
+    return out
+
+
 def mcmc_comparison(args):
     """ESS/s of the surrogate delayed-acceptance sampler against the plain
     engine sampler on this GPU (64 chains, the same proposal and start
@@ -339,6 +377,9 @@ def run_gw(args, world, rank, local, dist):
         v, cores, n, dt = cpu_baseline(wl, args.config, args.cpu_seconds)
         cpu = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
                "sample": f"{n} full evaluations (K=1) of all {wl.n_events} events, {dt:.1f} s"}
+    c3 = None
+    if rank == 0 and not args.no_variants:
+        c3 = c3_sweep(local)
     mc = None
     if rank == 0 and not args.no_mcmc and args.config == "c2":
         mc = mcmc_comparison(args)
@@ -366,6 +407,7 @@ def run_gw(args, world, rank, local, dist):
             "clocks": clk,
             "variants": variants,
             "event_dials_per_s": value * wl.n_dials,
+            "c3_batched_vs_k": c3,
             "mcmc": mc,
         }
         print(json.dumps(line), flush=True)

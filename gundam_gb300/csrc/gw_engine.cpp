@@ -109,6 +109,14 @@ struct gw_engine {
   bool weights_valid = false;
   bool use_graph = false;
   std::map<int, cudaGraphExec_t> graphs;
+  // gw_eval_device graphs, per (K, parameter / output pointers, stream)
+  std::map<std::vector<uintptr_t>, cudaGraphExec_t> dev_graphs;
+  void clear_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
+    for (auto& g : dev_graphs) cudaGraphExecDestroy(g.second);
+    dev_graphs.clear();
+  }
   std::vector<int32_t> sorted_to_result;
   gw_layout_info layout{};
   int64_t resident = 0;
@@ -119,7 +127,7 @@ struct gw_engine {
   int64_t kernel_launches = 0;
 
   ~gw_engine() {
-    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    clear_graphs();
     for (auto& pe : prof_events) {
       cudaEventDestroy(pe.first);
       cudaEventDestroy(pe.second);
@@ -464,8 +472,7 @@ extern "C" int gw_set_likelihood(gw_engine* e, int32_t t) {
     return fail(e, GW_ERR_ARG, "bad likelihood type %d", t);
   e->llh_type = t;
   e->view.llh_type = t;
-  for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
-  e->graphs.clear();
+  e->clear_graphs();
   return GW_OK;
 }
 
@@ -719,9 +726,7 @@ int build_and_upload(gw_engine* e) {
   }
 
   // 4. tiles
-  // default payload per tile: 23936 bytes, so that the K = 1 kernel's two
-  // stages (payload + headers + event data) keep three CTAs per SM
-  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : 23936) / (int64_t)tsz;
+  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : 24576) / (int64_t)tsz;
   cap_elems = std::min<int64_t>(cap_elems, kMaxPayloadElems);
   cap_elems = std::max<int64_t>(cap_elems, 64);
   std::vector<TilePlan> tiles;
@@ -904,8 +909,8 @@ int build_and_upload(gw_engine* e) {
   v.cap = e->cap;
   v.tile_payload_bytes = (int)(((cap_elems * tsz) + 127) & ~(int64_t)127);
 
-  // the K = 1 kernel copies a tile's headers, event info and base weights
-  // with bulk copies rounded out to 16-byte boundaries: pad each array
+  // slack after the per-dial and per-event arrays (reads rounded out to
+  // 16-byte boundaries stay inside the allocation)
   hdr.resize(hdr.size() + 2, 0);
   evinfo.resize(evinfo.size() + 8, 0);
   w0.resize(w0.size() + 4, T(0));
@@ -1206,7 +1211,32 @@ extern "C" int gw_eval_device(gw_engine* e, const double* d_params, int32_t K, d
   int rc = refresh_tables(e);
   if (rc) return rc;
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
-  rc = launch_chain(e, d_params, K, d_sums, d_sums2, d_llh, d_llh_stat, s);
+  if (e->use_graph) {
+    // the launch chain captured once per (K, pointers, stream) and replayed
+    const std::vector<uintptr_t> key = {(uintptr_t)K,       (uintptr_t)d_params, (uintptr_t)d_sums,
+                                        (uintptr_t)d_sums2, (uintptr_t)d_llh,    (uintptr_t)d_llh_stat,
+                                        (uintptr_t)s};
+    auto it = e->dev_graphs.find(key);
+    if (it == e->dev_graphs.end()) {
+      GW_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const int r = launch_chain(e, d_params, K, d_sums, d_sums2, d_llh, d_llh_stat, s);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+      }
+      if (ce != cudaSuccess) return fail(e, GW_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail(e, GW_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ie));
+      it = e->dev_graphs.emplace(key, ex).first;
+    }
+    GW_CUDA(e, cudaGraphLaunch(it->second, s));
+  } else {
+    rc = launch_chain(e, d_params, K, d_sums, d_sums2, d_llh, d_llh_stat, s);
+  }
   if (rc == GW_OK) e->weights_valid = e->copy_weights && K == 1;
   return rc;
 }
@@ -1276,8 +1306,7 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   e->shape = best_shape;
   e->batched_grid = best_grid;
   e->tuned = true;
-  for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
-  e->graphs.clear();
+  e->clear_graphs();
   return check_status(e);
 }
 
@@ -1293,8 +1322,7 @@ extern "C" int gw_set_shape(gw_engine* e, int32_t kind, int32_t kc, int32_t thre
     if (bps < 1) return fail(e, GW_ERR_ARG, "shape does not fit on an SM");
     e->shape = b;
     e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
-    for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
-    e->graphs.clear();
+    e->clear_graphs();
     return GW_OK;
   }
   return fail(e, GW_ERR_ARG, "no compiled shape (%d, %d, %d, %d)", kind, kc, threads, stages);
@@ -1320,8 +1348,7 @@ extern "C" int gw_set_event_weight_copy(gw_engine* e, int32_t enable) {
     e->resident += (int64_t)bytes;
   }
   e->copy_weights = enable != 0;
-  for (auto& g : e->graphs) cudaGraphExecDestroy(g.second);
-  e->graphs.clear();
+  e->clear_graphs();
   return GW_OK;
 }
 

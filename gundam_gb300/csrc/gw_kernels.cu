@@ -95,105 +95,48 @@ __global__ void k_table_fn(const DevView v, int K) {
 // ---------------------------------------------------------------------------
 // K = 1: type-ordered dial evaluation, one thread per dial.
 // ---------------------------------------------------------------------------
-// Per stage, after the payload: the tile's headers, event info and base
-// weights, each brought by its own bulk copy rounded out to 16-byte bounds
-// (the arrays are padded on the device), so nothing inside a tile waits on
-// a global load.
-constexpr int kPlainHdrBytes = 8 * (kMaxTileDials + 3);          // <= 1024 headers + rounding
-constexpr int kPlainEvBytes = 2 * (kMaxTileEvents + 16);         // <= 264 entries
-constexpr int kPlainW0Bytes = 8 * (kMaxTileEvents + 2);          // FP64 worst case
-constexpr int kPlainAuxBytes = ((kPlainHdrBytes + 15) & ~15) + ((kPlainEvBytes + 15) & ~15) + kPlainW0Bytes;
-
-struct PlainAux {
-  int hdr_shift, ev_shift, w0_shift;
-};
-
-// Issues the payload and the per-dial / per-event arrays of `td` into one
-// stage; returns the element shifts of the rounded-down copies.
-template <typename T>
-__device__ __forceinline__ PlainAux issue_plain_tile(const DevView& v, const TileDesc& td, unsigned char* stage,
-                                                     int TB, uint64_t* bar) {
-  PlainAux a;
-  const uint32_t pbytes = (uint32_t)td.payload_16b * 16u;
-  const uint32_t h0 = td.dial0 & ~1u, e0 = td.event0 & ~7u;
-  constexpr uint32_t wmask = sizeof(T) == 4 ? 3u : 1u;
-  const uint32_t w0i = td.event0 & ~wmask;
-  a.hdr_shift = (int)(td.dial0 - h0);
-  a.ev_shift = (int)(td.event0 - e0);
-  a.w0_shift = (int)(td.event0 - w0i);
-  const uint32_t hn = ((uint32_t)a.hdr_shift + td.ndials + 1u) & ~1u;
-  const uint32_t en = ((uint32_t)a.ev_shift + td.nevents + 7u) & ~7u;
-  const uint32_t wn = ((uint32_t)a.w0_shift + td.nevents + wmask) & ~wmask;
-  const uint32_t hb = hn * 8u, eb = en * 2u, wb = wn * (uint32_t)sizeof(T);
-  unsigned char* aux = stage + TB;
-  mbar_expect_tx(bar, pbytes + hb + eb + wb);
-  if (pbytes > 0) bulk_load(stage, v.payload + td.payload_off, pbytes, bar);
-  if (hb > 0) bulk_load(aux, v.hdr + h0, hb, bar);
-  if (eb > 0) bulk_load(aux + ((kPlainHdrBytes + 15) & ~15), v.evinfo + e0, eb, bar);
-  if (wb > 0)
-    bulk_load(aux + ((kPlainHdrBytes + 15) & ~15) + ((kPlainEvBytes + 15) & ~15), (const T*)v.w0 + w0i, wb, bar);
-  return a;
-}
-
-// A tile descriptor as two 16-byte words (kept in registers while prefetched).
-struct TileWords {
-  uint4 a, b;
-};
-
-__device__ __forceinline__ TileWords load_tile_words(const TileDesc* t) {
-  const uint4* p = reinterpret_cast<const uint4*>(t);
-  return TileWords{__ldg(p), __ldg(p + 1)};
-}
-
-__device__ __forceinline__ TileDesc tile_of(const TileWords& w) {
-  TileDesc t;
-  static_assert(sizeof(TileDesc) == sizeof(TileWords), "TileDesc layout");
-  memcpy(&t, &w, sizeof(t));
-  return t;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
-  const int SB = TB + kPlainAuxBytes;  // stage bytes
-  T* dval = (T*)(smem + 2 * SB);                              // [1024]
-  double* wsh = (double*)(smem + 2 * SB + 1024 * sizeof(T));  // [kMaxTileEvents]
-  uint16_t* sev = (uint16_t*)(wsh + kMaxTileEvents);          // [kMaxTileEvents]
+  unsigned char* stage0 = smem;
+  unsigned char* stage1 = smem + TB;
+  T* dval = (T*)(smem + 2 * TB);                       // [1024]
+  double* wsh = (double*)(smem + 2 * TB + 1024 * sizeof(T));  // [kMaxTileEvents]
+  uint16_t* sev = (uint16_t*)(wsh + kMaxTileEvents);  // [kMaxTileEvents]
   __shared__ uint64_t bar[2];
-  __shared__ TileDesc s_td[2];
-  __shared__ PlainAux s_aux[2];
   __shared__ int s_bstart[kMaxLocalBins], s_bend[kMaxLocalBins];
 
   const int tid = threadIdx.x;
-  int tile = blockIdx.x;
-  TileWords pref = {};  // thread 0: descriptor of the tile after the next (registers)
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
-    if (tile < v.n_tiles) {
-      const TileDesc t0 = tile_of(load_tile_words(v.tiles + tile));
-      s_td[0] = t0;
-      s_aux[0] = issue_plain_tile<T>(v, t0, smem, TB, &bar[0]);
-      if (tile + (int)gridDim.x < v.n_tiles) pref = load_tile_words(v.tiles + tile + gridDim.x);
-    }
   }
   __syncthreads();
 
+  int tile = blockIdx.x;
+  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
   for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
     const int st = it & 1;
     const uint32_t parity = (uint32_t)((it >> 1) & 1);
     const int next = tile + gridDim.x;
-    if (tid == 0 && next < v.n_tiles) {
-      const TileDesc tn = tile_of(pref);
-      s_td[st ^ 1] = tn;
-      s_aux[st ^ 1] = issue_plain_tile<T>(v, tn, smem + (st ^ 1) * SB, TB, &bar[st ^ 1]);
-      // used one iteration from now: the load's latency hides behind this tile
-      if (next + (int)gridDim.x < v.n_tiles) pref = load_tile_words(v.tiles + next + gridDim.x);
+    if (tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+
+    const TileDesc td = v.tiles[tile];
+    uint64_t h[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = tid + j * kPlainThreads;
+      h[j] = (i < td.ndials) ? v.hdr[td.dial0 + i] : 0ull;
     }
-    const TileDesc td = s_td[st];
-    const PlainAux ax = s_aux[st];
+    T w0 = T(1);
+    uint16_t evi = 0;
+    if (tid < td.nevents) {
+      evi = v.evinfo[td.event0 + tid];
+      w0 = ((const T*)v.w0)[td.event0 + tid];
+      sev[tid] = evi;
+    }
     if (tid < kMaxLocalBins) {
       s_bstart[tid] = 0;
       s_bend[tid] = 0;
@@ -206,27 +149,15 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
       }
       return;
     }
-    const unsigned char* sp = smem + st * SB;
-    const T* pl = (const T*)sp;
-    const uint64_t* shdr = (const uint64_t*)(sp + TB) + ax.hdr_shift;
-    const uint16_t* sevi = (const uint16_t*)(sp + TB + ((kPlainHdrBytes + 15) & ~15)) + ax.ev_shift;
-    const T* sw0 = (const T*)(sp + TB + ((kPlainHdrBytes + 15) & ~15) + ((kPlainEvBytes + 15) & ~15)) + ax.w0_shift;
+    const T* pl = (const T*)(st ? stage1 : stage0);
 
-    T w0 = T(1);
-    uint16_t evi = 0;
-    if (tid < td.nevents) {
-      evi = sevi[tid];
-      w0 = sw0[tid];
-      sev[tid] = evi;
-    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int i = tid + j * kPlainThreads;
       if (i < td.ndials) {
-        const uint64_t h = shdr[i];
         T val[1];
-        dial_values<T, 1>(v, h, pl, 0, 0, val);
-        dval[hdr_slot(h)] = val[0];
+        dial_values<T, 1>(v, h[j], pl, 0, 0, val);
+        dval[hdr_slot(h[j])] = val[0];
       }
     }
     __syncthreads();
@@ -337,7 +268,7 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
 // ---------------------------------------------------------------------------
 size_t plain_smem_bytes(const DevView& v) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
-  return 2 * ((size_t)v.tile_payload_bytes + kPlainAuxBytes) + 1024 * tsz + kMaxTileEvents * sizeof(double) +
+  return 2 * (size_t)v.tile_payload_bytes + 1024 * tsz + kMaxTileEvents * sizeof(double) +
          kMaxTileEvents * sizeof(uint16_t);
 }
 
