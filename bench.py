@@ -45,10 +45,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true")
-    ap.add_argument("--mcmc-steps", type=int, default=1500)
+    ap.add_argument("--mcmc-steps", type=int, default=3000)
     ap.add_argument("--mcmc-train", type=int, default=65536)
     ap.add_argument("--mcmc-epochs", type=int, default=50)
-    ap.add_argument("--mcmc-nsub", type=int, default=20)
+    ap.add_argument("--mcmc-nsub", type=int, default=40)
     return ap.parse_args()
 
 
@@ -303,8 +303,11 @@ def run_gw(args, world, rank, local, dist):
     import numpy as np
     import torch
 
+    import ctypes as C
+
     from gundam_gb300 import Engine, Workload
-    from gundam_gb300.roofline import algorithmic_bytes
+    from gundam_gb300 import _native as N
+    from gundam_gb300.roofline import algorithmic_bytes, algorithmic_flops
 
     torch.cuda.set_device(local)
     wl = Workload(args.config, n_events=args.events, seed=args.seed)
@@ -341,6 +344,15 @@ def run_gw(args, world, rank, local, dist):
     peak, peak_kind = peaks()
     alg = algorithmic_bytes(wl, args.precision, K)
     achieved = alg / (kernel_ms / 1e3) / 1e9
+    # the batched kernels serve K points per byte read: their binding
+    # resource is FP32 throughput, measured here with an FMA probe
+    fp32_peak = C.c_double(0.0)
+    N.libgw().gw_measure_fp32_peak(local, C.byref(fp32_peak))
+    flops = algorithmic_flops(wl, K)
+    compute = {"bound": "fp32", "unit": "TFLOP/s", "achieved": flops / (kernel_ms / 1e3) / 1e12,
+               "peak": fp32_peak.value, "peak_source": "measured on this GPU (FMA probe, gw_measure_fp32_peak)",
+               "frac": (flops / (kernel_ms / 1e3) / 1e12) / fp32_peak.value if fp32_peak.value > 0 else None,
+               "algorithmic_flops_per_launch": flops}
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
@@ -400,7 +412,7 @@ def run_gw(args, world, rank, local, dist):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": ("k_plain" if K == 1 else ("k_multi" if shape[0] == 1 else "k_batched")),
                          "kernel_ms": kernel_ms,
-                         "algorithmic_bytes_per_launch": alg},
+                         "algorithmic_bytes_per_launch": alg, "compute": compute},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,

@@ -159,6 +159,7 @@ GW_SIGNATURES: dict[str, list] = {
     "gw_set_profiling": [_P, _I32],
     "gw_llh_noalloc": [_P, _P, _P, _I32, _I32, _I32, _P, _P],
     "gw_selftest_wait_timeout": [C.c_uint32, _P],
+    "gw_measure_fp32_peak": [_I32, _P],
     "gwm_create": [_P, _I32, _I32, _I32, _P],
     "gwm_destroy": [_P],
     "gwm_last_error": [_P, C.c_char_p, C.c_size_t],

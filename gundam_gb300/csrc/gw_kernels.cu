@@ -15,6 +15,8 @@
 //               and reduce it, deterministically, to one value per point.
 // The reference needs ~1 + n_types + 2*(2 + log2 max bin occupancy) launches
 // for the same work (CacheWeights.cpp:153-183, CacheRecursiveSums.cpp:282-352).
+#include <algorithm>
+
 #include "gw.h"
 #include "gw_device.cuh"
 
@@ -434,5 +436,64 @@ extern "C" int gw_selftest_wait_timeout(uint32_t limit_us, int32_t* timed_out) {
   cudaFree(d);
   if (e != cudaSuccess) return GW_ERR_CUDA;
   *timed_out = (h == gw::kStatusCopyTimeout) ? 1 : 0;
+  return GW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 throughput probe (the denominator of the compute roofline of the
+// batched kernels): independent FMA chains in registers, no memory traffic
+// in the loop.
+// ---------------------------------------------------------------------------
+namespace gw {
+namespace {
+__global__ void __launch_bounds__(256) k_fma_probe(int iters, float b, float c, float* sink) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = (float)(threadIdx.x + j) * 1e-3f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fmaf(a[j], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 12345.678f) sink[0] = s;  // keeps the chains live
+}
+}  // namespace
+}  // namespace gw
+
+extern "C" int gw_measure_fp32_peak(int32_t device, double* tflops) {
+  if (!tflops) return GW_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return GW_ERR_CUDA;
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  float* sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return GW_ERR_NOMEM;
+  }
+  const int iters = 8192, blocks = sms * 8, threads = 256;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a);
+    gw::k_fma_probe<<<blocks, threads>>>(iters, 0.999f, 1e-4f, sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms > 0.f) best = std::max(best, 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return GW_ERR_CUDA;
+  *tflops = best;
   return GW_OK;
 }

@@ -1424,7 +1424,12 @@ __device__ __forceinline__ double u01(uint64_t h) { return ((double)(h >> 11) + 
 __global__ void k_propose_stage(const double* __restrict__ phi, int P, const float* __restrict__ Lt, uint64_t seed,
                                 uint64_t step, double* __restrict__ prop, const float* __restrict__ mean,
                                 const float* __restrict__ scale, float* __restrict__ x, bf16* __restrict__ h0) {
-  extern __shared__ float nrm[];
+  // blockDim.x = G * P32: group g of the column's partial sums covers the
+  // k-range [g*ks, (g+1)*ks); the groups are combined in a fixed order
+  extern __shared__ float shp[];
+  const int P32 = (P + 31) & ~31, G = blockDim.x / P32;
+  float* nrm = shp;            // [P + 1]
+  float* part = shp + P + 1;   // [G][P32]
   const int c = blockIdx.x;
   for (int k2 = threadIdx.x; 2 * k2 < P; k2 += blockDim.x) {
     const float u1 = (float)u01(hash4(seed, step, c, 2 * k2));
@@ -1436,18 +1441,27 @@ __global__ void k_propose_stage(const double* __restrict__ phi, int P, const flo
     if (2 * k2 + 1 < P) nrm[2 * k2 + 1] = r * sn;
   }
   __syncthreads();
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+  const int g = threadIdx.x / P32, p = threadIdx.x - g * P32;
+  const int ks = (P + G - 1) / G;
+  if (p < P) {
+    const int k0 = g * ks, k1 = min(min(P, (g + 1) * ks), p + 1);
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-    int k = 0;
-    for (; k + 4 <= p + 1; k += 4) {
+    int k = k0;
+    for (; k + 4 <= k1; k += 4) {
       a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
       a1 = fmaf(Lt[(size_t)(k + 1) * P + p], nrm[k + 1], a1);
       a2 = fmaf(Lt[(size_t)(k + 2) * P + p], nrm[k + 2], a2);
       a3 = fmaf(Lt[(size_t)(k + 3) * P + p], nrm[k + 3], a3);
     }
-    for (; k <= p; ++k) a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
+    for (; k < k1; ++k) a0 = fmaf(Lt[(size_t)k * P + p], nrm[k], a0);
+    part[g * P32 + p] = (a0 + a1) + (a2 + a3);
+  }
+  __syncthreads();
+  if (g == 0 && p < P) {
+    float inc = 0.f;
+    for (int q = 0; q < G; ++q) inc += part[q * P32 + p];
     const size_t o = (size_t)c * P + p;
-    const double v = phi[o] + (double)((a0 + a1) + (a2 + a3));
+    const double v = phi[o] + (double)inc;
     prop[o] = v;
     const float z = (float)((v - (double)mean[p]) / (double)scale[p]);
     x[o] = z;
@@ -1466,9 +1480,12 @@ __global__ void k_finish_accept(const double* __restrict__ part, int nblk, const
                                 const double* __restrict__ m, const float* __restrict__ icov, uint64_t seed,
                                 uint64_t step, int first, double* __restrict__ phi, double* __restrict__ f,
                                 int32_t* __restrict__ n_acc) {
+  // blockDim.x = G * P32 as k_propose_stage
   extern __shared__ float shf[];
-  float* d = shf;          // [P]
-  float* red = shf + P;    // [blockDim.x]
+  const int P32 = (P + 31) & ~31, G = blockDim.x / P32;
+  float* d = shf;              // [P32]
+  float* up = shf + P32;       // [G][P32]
+  float* red = up + G * P32;   // [P32]
   __shared__ double s_llh;
   __shared__ int s_take;
   const int c = blockIdx.x, lane = threadIdx.x & 31;
@@ -1478,29 +1495,36 @@ __global__ void k_finish_accept(const double* __restrict__ part, int nblk, const
     for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
     if (lane == 0) s_llh = t;
   }
-  double pen = 0.0;
+  const int g = threadIdx.x / P32, p = threadIdx.x - g * P32;
   if (m) {
-    for (int p = threadIdx.x; p < P; p += blockDim.x) d[p] = (float)(prop[(size_t)c * P + p] - m[p]);
+    if (g == 0) d[p] = p < P ? (float)(prop[(size_t)c * P + p] - m[p]) : 0.f;
     __syncthreads();
-    float acc = 0.f;
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    const int ks = (P + G - 1) / G;
+    if (p < P) {
+      const int k0 = g * ks, k1 = min(P, (g + 1) * ks);
       float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
-      int k = 0;
-      for (; k + 4 <= P; k += 4) {
+      int k = k0;
+      for (; k + 4 <= k1; k += 4) {
         u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
         u1 = fmaf(icov[(size_t)(k + 1) * P + p], d[k + 1], u1);
         u2 = fmaf(icov[(size_t)(k + 2) * P + p], d[k + 2], u2);
         u3 = fmaf(icov[(size_t)(k + 3) * P + p], d[k + 3], u3);
       }
-      for (; k < P; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
-      acc = fmaf(d[p], (u0 + u1) + (u2 + u3), acc);
+      for (; k < k1; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+      up[g * P32 + p] = (u0 + u1) + (u2 + u3);
     }
-    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (g == 0) {
+      float u = 0.f;
+      for (int q = 0; q < G; ++q) u += (p < P) ? up[q * P32 + p] : 0.f;
+      red[p] = d[p] * u;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    double pen = 0.0;
     if (m)
-      for (int i = 0; i < (int)blockDim.x; ++i) pen += (double)red[i];
+      for (int i = 0; i < P32; ++i) pen += (double)red[i];
     const double fn = s_llh + pen;
     int take;
     if (first) {
@@ -1518,7 +1542,7 @@ __global__ void k_finish_accept(const double* __restrict__ part, int nblk, const
   }
   __syncthreads();
   if (s_take)
-    for (int p = threadIdx.x; p < P; p += blockDim.x) phi[(size_t)c * P + p] = prop[(size_t)c * P + p];
+    for (int q = threadIdx.x; q < P; q += blockDim.x) phi[(size_t)c * P + q] = prop[(size_t)c * P + q];
 }
 
 }  // namespace
@@ -1567,6 +1591,7 @@ extern "C" int gwm_set_chain(gwm_net* n, const double* prop_chol, const double* 
   if (!n || !prop_chol || ((prior_mean == nullptr) != (prior_icov == nullptr)))
     return gwm_fail(n, GW_ERR_ARG, "gwm_set_chain: bad arguments");
   if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_set_chain: gwm_set_head first");
+  if (n->dims[0] > 1024) return gwm_fail(n, GW_ERR_LIMIT, "gwm_set_chain: at most 1024 parameters");
   GWM_CUDA(n, cudaSetDevice(n->device));
   GWM_CUDA(n, cudaStreamSynchronize(n->stream));
   const int P = n->dims[0], Cm = n->batch_max;
@@ -1618,9 +1643,13 @@ extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, 
   GWM_CUDA(n, cudaSetDevice(n->device));
   const int P = s->P;
   const int Bp = ((C + 7) / 8) * 8;
-  const unsigned thr = P >= 256 ? 256 : (unsigned)(((P + 31) / 32) * 32);
+  // G thread groups of P32 threads per chain split the k-range of the
+  // proposal and penalty mat-vecs
+  const int P32 = (P + 31) & ~31;
+  const int G = std::max(1, std::min(4, 1024 / P32));
+  const unsigned thr = (unsigned)(G * P32);
   const bool prior = s->prior;
-  const size_t sh_prop = sizeof(float) * (size_t)(P + 1);
+  const size_t sh_prop = sizeof(float) * ((size_t)P + 1 + (size_t)G * P32);
   GWM_CUDA(n, cudaMemcpyAsync(s->phi, theta0, sizeof(double) * (size_t)C * P, cudaMemcpyHostToDevice, n->stream));
   GWM_CUDA(n, cudaMemsetAsync(s->nacc, 0, sizeof(int32_t) * C, n->stream));
   // rows C..Bp of the staging buffer stay finite (zeros)
@@ -1628,7 +1657,7 @@ extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, 
     GWM_CUDA(n, cudaMemsetAsync(n->h_theta + (size_t)C * P, 0, sizeof(double) * (size_t)(Bp - C) * P, n->stream));
   int rc = GW_OK;
   const int nbx = (n->dims[n->n_layers] + 31) / 32;
-  const size_t sh_fin = sizeof(float) * ((size_t)P + thr);
+  const size_t sh_fin = sizeof(float) * ((size_t)P32 * (G + 2));
   if (f0) {
     GWM_CUDA(n, cudaMemcpyAsync(s->f, f0, sizeof(double) * C, cudaMemcpyHostToDevice, n->stream));
   } else {

@@ -199,11 +199,13 @@ class Engine:
     # ---- convenience: load a generated workload ----
     @classmethod
     def from_workload(cls, wl, precision="fp64", k_max=1, llh_type=None, prior=True, device=0, tile_bytes=0,
-                      per_dial=False) -> "Engine":
+                      per_dial=False, initialize=True) -> "Engine":
         """Builds an engine holding `wl` the way Cache::Manager::Update fills its caches.
 
         per_dial=True issues one call per dial (the reference's AddSpline /
-        AddGraph / ... sequence); otherwise one batched gw_add_dials call."""
+        AddGraph / ... sequence); otherwise one batched gw_add_dials call.
+        initialize=False stops before gw_initialize (the engine holds its own
+        copies by then, so a large workload can be released first)."""
         e = cls(wl.n_events, wl.n_params, wl.n_bins, k_max=k_max, precision=precision, device=device,
                 tile_bytes=tile_bytes)
         for p in range(wl.n_params):
@@ -239,7 +241,8 @@ class Engine:
         e.set_likelihood(llh_type)
         if prior:
             e.set_prior(wl.prior_mean, wl.prior_icov)
-        e.initialize()
+        if initialize:
+            e.initialize()
         return e
 
 

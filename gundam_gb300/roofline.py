@@ -33,3 +33,30 @@ def algorithmic_bytes(wl, precision: str, K: int) -> int:
     tables = int(wl.table_size.sum()) * s if wl.n_tables else 0
     D, Nev, P, B = wl.n_dials, wl.n_events, wl.n_params, wl.n_bins
     return payload + D * 6 + Nev * (4 + s + 4) + tables + K * (P * 8 + B * 16)
+
+
+# FP32 operations per dial and point, counted on the restated formulas
+# (Hermite spline: index, fraction, cubic; graph: search + linear; bilinear:
+# three linear interpolations), plus one multiply per dial for the event
+# product and, per event and point, the cap, the base weight and the FP64
+# w and w^2 accumulations (counted as 4).
+FLOPS_PER_DIAL = {
+    N.GW_DIAL_NORM: 1, N.GW_DIAL_MONOTONIC: 30, N.GW_DIAL_UNIFORM: 20, N.GW_DIAL_GENERAL: 35,
+    N.GW_DIAL_COMPACT: 30, N.GW_DIAL_GRAPH: 12, N.GW_DIAL_BILINEAR: 20, N.GW_DIAL_BICUBIC: 60,
+    N.GW_DIAL_TABULATED: 3,
+}
+
+
+def algorithmic_flops(wl, K: int) -> int:
+    """FP32-equivalent operations of one pass over all events for K points."""
+    t = wl.dial_type.astype(np.int64)
+    counts = np.bincount(t, minlength=16)
+    per_point = 0
+    for typ, f in FLOPS_PER_DIAL.items():
+        per_point += int(counts[typ]) * (f + 1)
+    kr = t == N.GW_DIAL_KRIGED
+    if kr.any():
+        lens = np.diff(wl.dial_data_start)[kr]
+        per_point += int(((lens - 2) // 2).sum()) * 2 + int(kr.sum())
+    per_point += wl.n_events * 4
+    return per_point * K

@@ -271,6 +271,11 @@ int gw_llh_noalloc(const double* d_sums, const double* d_sums2, const double* d_
  * as the limit.  timed_out = 1 when the wait gave up and reported it. */
 int gw_selftest_wait_timeout(uint32_t limit_us, int32_t* timed_out);
 
+/* FP32 FMA throughput of the device in TFLOP/s (independent FMA chains in
+ * registers, best of four launches): the denominator of the compute roofline
+ * of the batched kernels.  No reference counterpart. */
+int gw_measure_fp32_peak(int32_t device, double* tflops);
+
 /* Layout facts for measurement: tiles, dials, payload bytes, algorithmic
  * bytes read per evaluation pass. */
 typedef struct gw_layout_info {
@@ -349,7 +354,7 @@ int gwm_train_epochs(gwm_net* net, int32_t epochs, int32_t batch, float lr0, flo
  * (GUNDAM's -2 log L convention; accept when log u < -(f' - f) / 2).
  * gwm_set_chain: proposal Cholesky factor L [P x P] (lower, row-major) and the
  * Gaussian prior (mean [P], inverse covariance [P x P]; both null: none),
- * P = dims[0].  gwm_substeps: n_sub steps for C <= batch_max chains from
+ * P = dims[0] <= 1024.  gwm_substeps: n_sub steps for C <= batch_max chains from
  * theta0 [C x P] with values f0 [C] (null: evaluated first); writes the end
  * points phi [C x P], fphi [C] and the accepted sub-steps n_acc [C] (optional).
  * Normals and uniforms come from a counter-based hash of (seed, step, chain). */

@@ -135,3 +135,68 @@ def ref_lib():
             f.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, _P, C.c_int]
             f.restype = C.c_double
     return _ref
+
+
+REF_CACHE = REF.parent / "libref_cache.so"
+_ref_cache = None
+
+
+def ref_cache_lib():
+    """GUNDAM's own Cache::Manager calculators compiled for the host (only
+    where oracle/_ref was built from the reference tree)."""
+    global _ref_cache
+    if _ref_cache is None and REF_CACHE.exists():
+        lib_ = C.CDLL(str(REF_CACHE), mode=C.RTLD_GLOBAL | os.RTLD_NOW)
+        lib_.ref_cache_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int64] + [_P] * 13
+        lib_.ref_cache_create.restype = C.c_int
+        lib_.ref_cache_eval.argtypes = [_P, _P, _P, _P, _P]
+        lib_.ref_cache_eval.restype = C.c_int
+        lib_.ref_cache_error.argtypes = [_P]
+        lib_.ref_cache_error.restype = C.c_char_p
+        lib_.ref_cache_destroy.argtypes = [_P]
+        lib_.ref_cache_destroy.restype = None
+        _ref_cache = lib_
+    return _ref_cache
+
+
+class RefCache:
+    """The reference's Cache::Weights + Cache::RecursiveSums filled from a
+    Workload through its own operator API (oracle/ref/ref_cache.cpp)."""
+
+    def __init__(self, wl):
+        L = ref_cache_lib()
+        if L is None:
+            raise RuntimeError("oracle/_ref/libref_cache.so is not built")
+        self.wl = wl
+        self._keep = [np.ascontiguousarray(a) for a in (
+            wl.dial_type, wl.dial_result(), wl.dial_par0, wl.dial_par1, wl.dial_data_start, wl.dial_data,
+            wl.event_w0, wl.event_bin, wl.clamp_lo, wl.clamp_hi, wl.mirror_lo, wl.mirror_hi)]
+        t, r, p0, p1, ds, d, w0, b, clo, chi, mlo, mhi = self._keep
+        h = C.c_void_p()
+        rc = L.ref_cache_create(wl.n_events, wl.n_params, wl.n_bins, wl.n_dials, _p(t), _p(r.astype(np.int32)),
+                                _p(p0), _p(p1), _p(ds), _p(d), _p(w0), _p(b), _p(clo), _p(chi), _p(mlo), _p(mhi),
+                                C.byref(h))
+        if rc:
+            raise RuntimeError(f"ref_cache_create: {L.ref_cache_error(None).decode()}")
+        self._h = h
+
+    def eval(self, params, weights=False):
+        L = ref_cache_lib()
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        s = np.empty(self.wl.n_bins)
+        s2 = np.empty(self.wl.n_bins)
+        w = np.empty(self.wl.n_events) if weights else None
+        if L.ref_cache_eval(self._h, _p(p), _p(s), _p(s2), _p(w)):
+            raise RuntimeError(f"ref_cache_eval: {L.ref_cache_error(self._h).decode()}")
+        return (s, s2, w) if weights else (s, s2)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            ref_cache_lib().ref_cache_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

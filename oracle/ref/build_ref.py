@@ -1,9 +1,15 @@
-"""Builds oracle/_ref/libref_dials.so from the reference's own dial headers.
+"""Builds, from the reference's own sources where they lie, two host
+libraries into oracle/_ref/ (never committed; test infrastructure):
+
+* libref_dials.so: the per-dial response functions (src/Utils/include/
+  Calculate*.h, header-only) behind oracle/ref/ref_dials.cpp;
+* libref_cache.so: GUNDAM's Cache::Manager calculators compiled for the host
+  (src/CacheManager/src/{CacheParameters, CacheWeights, WeightBase,
+  WeightNormalization, Weight*Spline, WeightGraph, WeightBilinear,
+  CacheRecursiveSums, CacheAtomicCAS}.cpp with HEMI_CUDA_DISABLE and the
+  stand-in headers of oracle/ref/stubs/) behind oracle/ref/ref_cache.cpp.
 
 Usage: python oracle/ref/build_ref.py <path of the GUNDAM source tree>
-
-Only the header directory src/Utils/include of that tree is read (with -I);
-the output goes to oracle/_ref/ and is never committed.
 """
 import subprocess
 import sys
@@ -20,6 +26,15 @@ def main(reference: str) -> None:
     OUT.mkdir(exist_ok=True)
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w",
            "-I", str(inc), str(HERE / "ref_dials.cpp"), "-o", str(OUT / "libref_dials.so")]
+    subprocess.run(cmd, check=True)
+    cm = Path(reference) / "src" / "CacheManager"
+    units = ["CacheParameters", "CacheWeights", "WeightBase", "WeightNormalization", "WeightMonotonicSpline",
+             "WeightUniformSpline", "WeightGeneralSpline", "WeightCompactSpline", "WeightGraph", "WeightBilinear",
+             "CacheRecursiveSums", "CacheAtomicCAS"]
+    srcs = [str(cm / "src" / f"{u}.cpp") for u in units]
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-DHEMI_CUDA_DISABLE",
+           "-I", str(HERE / "stubs"), "-I", str(cm / "include"), "-I", str(inc),
+           str(HERE / "ref_cache.cpp"), *srcs, "-o", str(OUT / "libref_cache.so")]
     subprocess.run(cmd, check=True)
 
 

@@ -1,0 +1,2 @@
+// Empty stand-in: nothing of it is used by the host calculators.
+#pragma once

@@ -317,3 +317,23 @@ def test_device_pointer_entry_point(c1, c1_oracle):
     assert _bin_rel(d_s.cpu().numpy(), ref["sums"]) <= FP64_BIN_REL
     assert np.max(np.abs(d_l.cpu().numpy() - ref["llh"])) <= FP64_LLH_ABS
     eng.close()
+
+
+@pytest.mark.parametrize("name,cfg,events", [("c1", "c1", 0), ("c2s", "c2", 20000)])
+def test_engine_matches_reference_cache_manager_fixtures(name, cfg, events):
+    """Per-bin sums of the engine (FP64 and FP32 modes) against GUNDAM's own
+    Cache::Manager calculators (tests/golden/cache_sums.npz); empty bins are
+    0 here and the next bin's content there (documented difference)."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "cache_sums.npz")
+    wl = Workload(cfg, n_events=events, seed=2)
+    pts = g[f"{name}_points"]
+    occ = np.bincount(wl.event_bin, minlength=wl.n_bins) > 0
+    for prec, tol in (("fp64", 1e-12), ("fp32", 2e-5)):
+        eng = Engine.from_workload(wl, precision=prec, k_max=len(pts))
+        s, s2, _, _ = eng.eval(pts)
+        for got, ref in ((s, g[f"{name}_sums"]), (s2, g[f"{name}_sums2"])):
+            rel = np.abs(got - ref)[:, occ] / np.abs(ref[:, occ])
+            assert rel.max() < tol, (name, prec, rel.max())
+            assert np.all(got[:, ~occ] == 0.0)
+        eng.close()
