@@ -365,16 +365,18 @@ def run_gw(args, world, rank, local, dist):
     variants = {}
     if not args.no_variants:
         # the same engine at K=1 (plain kernel), and the FP64 engine at K=1
+        eng.autotune(1)
         ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-        variants[f"{args.precision}_K1"] = {
+        variants[f"{args.precision}_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
             "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9}
         if args.precision == "fp32":
             eng.close()
             eng = Engine.from_workload(wl, precision="fp64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
                                        device=local)
+            eng.autotune(1)
             ms64, kms64, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-            variants["fp64_K1"] = {
+            variants["fp64_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
                 "evals_per_s": 1e3 / ms64, "ms_per_eval": ms64, "kernel_ms": kms64,
                 "kernel_gbs": algorithmic_bytes(wl, "fp64", 1) / (kms64 / 1e3) / 1e9}
             if K > 1:

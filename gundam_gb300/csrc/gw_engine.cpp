@@ -1041,8 +1041,14 @@ int build_and_upload(gw_engine* e) {
   for (const DialRec& r : e->dials) L.dials_by_type[r.type]++;
 
   GW_CUDA(e, prepare_params(v));
-  // grids
-  const int bps = plain_blocks_per_sm(v);
+  // grids; the warp-specialised K = 1 kernel is the default (measured faster
+  // on every configuration; gw_autotune(e, 1) re-checks)
+  v.plain_kind = 1;
+  int bps = plain_blocks_per_sm(v);
+  if (bps < 1) {
+    v.plain_kind = 0;
+    bps = plain_blocks_per_sm(v);
+  }
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
   e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bps * e->num_sms));
   const int K0 = e->cfg.k_max;
@@ -1255,10 +1261,51 @@ extern "C" int gw_use_graph(gw_engine* e, int32_t on) {
   return GW_OK;
 }
 
+// K = 1: times both K = 1 kernels and keeps the faster.
+static int autotune_plain(gw_engine* e) {
+  std::vector<double> pts((size_t)e->cfg.n_params);
+  for (size_t i = 0; i < pts.size(); ++i) pts[i] = 0.001 * (double)((i * 7919) % 17) - 0.008;
+  GW_CUDA(e, cudaMemcpy(e->d_params, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice));
+  cudaEvent_t a, b;
+  GW_CUDA(e, cudaEventCreate(&a));
+  GW_CUDA(e, cudaEventCreate(&b));
+  float best = 1e30f;
+  int best_kind = e->view.plain_kind;
+  for (int kind = 0; kind < 2; ++kind) {
+    if (gw_set_plain_kernel(e, kind) != GW_OK) continue;
+    int rc = launch_chain(e, (const double*)e->d_params, 1, (double*)e->d_sums, (double*)e->d_sums2,
+                          (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
+    if (rc) return rc;
+    GW_CUDA(e, cudaEventRecord(a, e->stream));
+    for (int rep = 0; rep < 5; ++rep) {
+      rc = launch_chain(e, (const double*)e->d_params, 1, (double*)e->d_sums, (double*)e->d_sums2,
+                        (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
+      if (rc) return rc;
+    }
+    GW_CUDA(e, cudaEventRecord(b, e->stream));
+    GW_CUDA(e, cudaEventSynchronize(b));
+    float ms = 0;
+    GW_CUDA(e, cudaEventElapsedTime(&ms, a, b));
+    if (ms < best) {
+      best = ms;
+      best_kind = kind;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  int rc = gw_set_plain_kernel(e, best_kind);
+  if (rc) return rc;
+  return check_status(e);
+}
+
 extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   if (!e) return GW_ERR_ARG;
   if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
-  if (K < 2 || K > e->cfg.k_max) return fail(e, GW_ERR_ARG, "autotune needs 2 <= K <= k_max");
+  if (K == 1) {
+    GW_CUDA(e, cudaSetDevice(e->device));
+    return autotune_plain(e);
+  }
+  if (K < 1 || K > e->cfg.k_max) return fail(e, GW_ERR_ARG, "autotune needs 1 <= K <= k_max");
   GW_CUDA(e, cudaSetDevice(e->device));
   // deterministic synthetic points: all parameters at 0 except tiny offsets
   std::vector<double> pts((size_t)K * e->cfg.n_params);
@@ -1326,6 +1373,28 @@ extern "C" int gw_set_shape(gw_engine* e, int32_t kind, int32_t kc, int32_t thre
     return GW_OK;
   }
   return fail(e, GW_ERR_ARG, "no compiled shape (%d, %d, %d, %d)", kind, kc, threads, stages);
+}
+
+extern "C" int gw_set_plain_kernel(gw_engine* e, int32_t kind) {
+  if (!e || kind < 0 || kind > 1) return GW_ERR_ARG;
+  if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
+  GW_CUDA(e, cudaSetDevice(e->device));
+  const int old = e->view.plain_kind;
+  e->view.plain_kind = kind;
+  const int bps = plain_blocks_per_sm(e->view);
+  if (bps < 1) {
+    e->view.plain_kind = old;
+    return fail(e, GW_ERR_ARG, "K = 1 kernel %d does not fit on an SM", kind);
+  }
+  e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
+  e->clear_graphs();
+  return GW_OK;
+}
+
+extern "C" int gw_get_plain_kernel(const gw_engine* e, int32_t* kind) {
+  if (!e || !kind) return GW_ERR_ARG;
+  *kind = e->view.plain_kind;
+  return GW_OK;
 }
 
 extern "C" int gw_get_shape(const gw_engine* e, int32_t* kind, int32_t* kc, int32_t* threads, int32_t* stages) {

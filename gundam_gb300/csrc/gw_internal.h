@@ -16,6 +16,7 @@ enum : uint32_t {
 // Every device pointer and size a launch needs.  Plain data, passed by value.
 struct DevView {
   int precision;        // 0 = FP64, 1 = FP32
+  int plain_kind;       // K = 1 kernel: 0 = k_plain, 1 = k_plain_ws (warp-specialised)
   int n_params;
   int n_bins;
   int n_events;

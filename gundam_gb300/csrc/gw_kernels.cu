@@ -205,6 +205,142 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 }
 
 // ---------------------------------------------------------------------------
+// K = 1, warp-specialised.  Warps 0..5 (evaluators) evaluate the type-ordered
+// dials of a tile into one of two dial-value buffers while warps 6..7
+// (reducers) form the ordered products and the bin partials of the previous
+// tile from the other buffer, so the serial per-tile phases run beside the
+// next tile's evaluation instead of behind a block barrier.  Hand-over by
+// named barriers, per buffer b: FULL_b (evaluators arrive, reducers wait) and
+// EMPTY_b (reducers arrive, evaluators wait); EVAL among the evaluators
+// before a payload stage is refilled, RED among the reducers.  Every CTA runs
+// the same number of iterations on both sides, so the hand-over cannot
+// deadlock; a timed-out copy marks the block failed and the protocol runs on
+// without work.
+// ---------------------------------------------------------------------------
+constexpr int kWsEval = 192, kWsRed = 64;
+constexpr int kBarEval = 1, kBarFull = 2, kBarEmpty = 4, kBarRed = 6;
+
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPlainThreads) k_plain_ws(const DevView v) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int TB = v.tile_payload_bytes;
+  T* dval = (T*)(smem + 2 * TB);                          // [2][1024]
+  double* wsh = (double*)(smem + 2 * TB + 2048 * sizeof(T));  // [kMaxTileEvents]
+  uint16_t* sev = (uint16_t*)(wsh + kMaxTileEvents);      // [kMaxTileEvents]
+  __shared__ uint64_t bar[2];
+  __shared__ int s_bstart[kMaxLocalBins], s_bend[kMaxLocalBins];
+  __shared__ volatile int s_fail;
+
+  const int tid = threadIdx.x;
+  const int ntile = (int)blockIdx.x < v.n_tiles ? (v.n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                                                : 0;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    s_fail = 0;
+    if (ntile > 0) issue_tile(v, blockIdx.x, smem, &bar[0]);
+    if (ntile > 1) issue_tile(v, blockIdx.x + gridDim.x, smem + TB, &bar[1]);
+  }
+  __syncthreads();
+
+  if (tid < kWsEval) {
+    for (int it = 0; it < ntile; ++it) {
+      const int tile = blockIdx.x + it * gridDim.x;
+      const int st = it & 1;
+      const TileDesc td = v.tiles[tile];
+      uint64_t h[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        const int i = tid + j * kWsEval;
+        h[j] = (i < td.ndials) ? v.hdr[td.dial0 + i] : 0ull;
+      }
+      const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)((it >> 1) & 1), kWaitLimitNs);
+      if (!ok) s_fail = 1;
+      if (it >= 2) named_sync(kBarEmpty + st, kPlainThreads);  // the reducers are done with buffer st
+      T* dv = dval + st * 1024;
+      if (ok) {
+        const T* pl = (const T*)(smem + st * TB);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+          const int i = tid + j * kWsEval;
+          if (i < td.ndials) {
+            T val[1];
+            dial_values<T, 1>(v, h[j], pl, 0, 0, val);
+            dv[hdr_slot(h[j])] = val[0];
+          }
+        }
+      }
+      named_arrive(kBarFull + st, kPlainThreads);
+      named_sync(kBarEval, kWsEval);  // stage st fully read
+      if (tid == 0 && it + 2 < ntile) issue_tile(v, tile + 2 * gridDim.x, smem + st * TB, &bar[st]);
+    }
+  } else {
+    const int r = tid - kWsEval;
+    const int rwarp = r >> 5, lane = r & 31;
+    for (int it = 0; it < ntile; ++it) {
+      const int tile = blockIdx.x + it * gridDim.x;
+      const int b = it & 1;
+      const TileDesc td = v.tiles[tile];
+      for (int e = r; e < td.nevents; e += kWsRed) sev[e] = v.evinfo[td.event0 + e];
+      if (r < kMaxLocalBins) {
+        s_bstart[r] = 0;
+        s_bend[r] = 0;
+      }
+      named_sync(kBarRed, kWsRed);
+      named_sync(kBarFull + b, kPlainThreads);  // buffer b holds this tile's values
+      const T* dv = dval + b * 1024;
+      for (int e = r; e < td.nevents; e += kWsRed) {
+        const uint16_t evi = sev[e];
+        const int s0 = ev_slot(evi);
+        const int s1 = (e + 1 < td.nevents) ? ev_slot(sev[e + 1]) : (int)td.ndials;
+        T w = T(1);
+        for (int q = s0; q < s1; ++q) w *= dv[q];
+        if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
+        w = ((const T*)v.w0)[td.event0 + e] * w;
+        wsh[e] = (double)w;
+        if (v.event_weights) v.event_weights[v.sorted_to_result[td.event0 + e]] = (double)w;
+        const int lb = ev_lbin(evi);
+        if (e == 0 || ev_lbin(sev[e - 1]) != lb) s_bstart[lb] = e;
+        if (e + 1 == td.nevents || ev_lbin(sev[e + 1]) != lb) s_bend[lb] = e + 1;
+      }
+      named_arrive(kBarEmpty + b, kPlainThreads);  // buffer b consumed
+      named_sync(kBarRed, kWsRed);
+      // one warp per local bin (two warps: bins w, w + 2): fixed-order FP64 sums
+      for (int lb = rwarp; lb < (int)td.nbins; lb += 2) {
+        const int b0 = s_bstart[lb], b1 = s_bend[lb];
+        if (b1 > b0) {
+          double sw = 0.0, sw2 = 0.0;
+          for (int e = b0 + lane; e < b1; e += 32) {
+            const double w = wsh[e];
+            sw += w;
+            sw2 += w * w;
+          }
+          for (int o = 16; o; o >>= 1) {
+            sw += __shfl_xor_sync(0xffffffffu, sw, o);
+            sw2 += __shfl_xor_sync(0xffffffffu, sw2, o);
+          }
+          if (lane == 0) {
+            const int slot = (lb == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + lb];
+            v.partials[(size_t)slot * v.kpad] = make_double2(sw, sw2);
+          }
+        }
+      }
+      named_sync(kBarRed, kWsRed);  // sev, wsh and the markers are reused
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && s_fail) atomicOr(v.status, kStatusCopyTimeout);
+}
+
+// ---------------------------------------------------------------------------
 // Bin sums and likelihood.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double* sums, double* sums2,
@@ -270,7 +406,8 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
 // ---------------------------------------------------------------------------
 size_t plain_smem_bytes(const DevView& v) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
-  return 2 * (size_t)v.tile_payload_bytes + 1024 * tsz + kMaxTileEvents * sizeof(double) +
+  const size_t dv = (v.plain_kind == 1 ? 2048 : 1024) * tsz;
+  return 2 * (size_t)v.tile_payload_bytes + dv + kMaxTileEvents * sizeof(double) +
          kMaxTileEvents * sizeof(uint16_t);
 }
 
@@ -288,8 +425,8 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
 }
 
 template <typename T>
-static const void* plain_fn() {
-  return (const void*)k_plain<T>;
+static const void* plain_fn(int kind) {
+  return kind == 1 ? (const void*)k_plain_ws<T> : (const void*)k_plain<T>;
 }
 
 // Every batched shape: the lanes-over-points family (gw_lanes.cu), then the
@@ -323,7 +460,7 @@ static const ShapeEntry* find_shape(const BatchedShape& b) {
 }
 
 static const void* pick_plain(const DevView& v) {
-  return v.precision ? plain_fn<float>() : plain_fn<double>();
+  return v.precision ? plain_fn<float>(v.plain_kind) : plain_fn<double>(v.plain_kind);
 }
 
 int plain_blocks_per_sm(const DevView& v) {
@@ -380,10 +517,17 @@ cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t
 
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
   const size_t smem = plain_smem_bytes(v);
-  if (v.precision)
-    k_plain<float><<<grid, kPlainThreads, smem, s>>>(v);
-  else
-    k_plain<double><<<grid, kPlainThreads, smem, s>>>(v);
+  if (v.plain_kind == 1) {
+    if (v.precision)
+      k_plain_ws<float><<<grid, kPlainThreads, smem, s>>>(v);
+    else
+      k_plain_ws<double><<<grid, kPlainThreads, smem, s>>>(v);
+  } else {
+    if (v.precision)
+      k_plain<float><<<grid, kPlainThreads, smem, s>>>(v);
+    else
+      k_plain<double><<<grid, kPlainThreads, smem, s>>>(v);
+  }
   return cudaGetLastError();
 }
 

@@ -156,6 +156,13 @@ class Engine:
     def set_shape(self, kind, points_per_pass, threads, stages):
         self._chk(self.lib.gw_set_shape(self._e, kind, points_per_pass, threads, stages))
 
+    def set_plain_kernel(self, kind): self._chk(self.lib.gw_set_plain_kernel(self._e, int(kind)))
+
+    def plain_kernel(self) -> int:
+        k = C.c_int32()
+        self._chk(self.lib.gw_get_plain_kernel(self._e, C.byref(k)))
+        return k.value
+
     def set_event_weight_copy(self, on=True): self._chk(self.lib.gw_set_event_weight_copy(self._e, int(on)))
 
     def event_weights(self) -> np.ndarray:

@@ -337,3 +337,26 @@ def test_engine_matches_reference_cache_manager_fixtures(name, cfg, events):
             assert rel.max() < tol, (name, prec, rel.max())
             assert np.all(got[:, ~occ] == 0.0)
         eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_both_k1_kernels_agree_bit_for_bit(mixed, prec):
+    """k_plain and the warp-specialised k_plain_ws form the same products and
+    sums in the same order: identical results, per-event weights included;
+    gw_autotune(1) picks one of them."""
+    eng = Engine.from_workload(mixed, precision=prec, k_max=4)
+    eng.set_event_weight_copy(True)
+    pt = mixed.draw_points(1, 41)
+    out = []
+    for kind in (0, 1):
+        eng.set_plain_kernel(kind)
+        assert eng.plain_kernel() == kind
+        r = eng.eval(pt)
+        out.append([np.array(x, copy=True) for x in r] + [eng.event_weights().copy()])
+    for x, y in zip(out[0], out[1]):
+        np.testing.assert_array_equal(x, y)
+    eng.autotune(1)
+    assert eng.plain_kernel() in (0, 1)
+    r = eng.eval(pt)
+    np.testing.assert_array_equal(r[0], out[0][0])
+    eng.close()
