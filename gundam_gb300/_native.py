@@ -144,6 +144,7 @@ GW_SIGNATURES: dict[str, list] = {
     "gw_set_data": [_P, _P, _I32],
     "gw_set_likelihood": [_P, _I32],
     "gw_set_prior": [_P, _P, _P],
+    "gw_add_eigen_block": [_P, _I32, _I32, _P],
     "gw_initialize": [_P],
     "gw_eval": [_P, _P, _I32, _P, _P, _P, _P],
     "gw_eval_device": [_P, _P, _I32, _P, _P, _P, _P, _P],

@@ -84,6 +84,11 @@ struct gw_engine {
   int32_t llh_type = GW_LLH_NONE;
   std::vector<double> prior_mean, prior_icov;
   bool has_prior = false;
+  struct EigenBlock {
+    int first, n;
+    std::vector<double> V;
+  };
+  std::vector<EigenBlock> eigen;
 
   // ---- device state ----
   int device = 0;
@@ -486,6 +491,23 @@ extern "C" int gw_set_prior(gw_engine* e, const double* mean, const double* icov
   e->prior_mean.assign(mean, mean + P);
   e->prior_icov.assign(icov, icov + P * P);
   e->has_prior = true;
+  return GW_OK;
+}
+
+// ParameterSet eigen decomposition (ParameterSet.cpp:766-780,
+// ParametersManager::convertEigenToOrig, ParametersManager.cpp:329-334):
+// parameters [first, first + n) are given in the eigen basis and the engine
+// forms original = V * given on the device before mirroring and the dials.
+extern "C" int gw_add_eigen_block(gw_engine* e, int32_t first, int32_t n, const double* V) {
+  GW_REQUIRE_BUILDER(e);
+  if (!V || n < 1 || first < 0 || first + n > e->cfg.n_params)
+    return fail(e, GW_ERR_ARG, "eigen block [%d, %d) outside the %d parameters", first, first + n, e->cfg.n_params);
+  for (const auto& b : e->eigen)
+    if (first < b.first + b.n && b.first < first + n)
+      return fail(e, GW_ERR_ARG, "eigen block [%d, %d) overlaps [%d, %d)", first, first + n, b.first, b.first + b.n);
+  for (int64_t i = 0; i < (int64_t)n * n; ++i)
+    if (!std::isfinite(V[i])) return fail(e, GW_ERR_NOT_FINITE, "eigen block matrix is not finite");
+  e->eigen.push_back({first, n, std::vector<double>(V, V + (size_t)n * n)});
   return GW_OK;
 }
 
@@ -952,6 +974,26 @@ int build_and_upload(gw_engine* e) {
     v.prior_mean = (const double*)p;
     if ((rc = upload(e->prior_icov.data(), sizeof(double) * (size_t)P * P, &p))) return rc;
     v.prior_icov = (const double*)p;
+  }
+  if (!e->eigen.empty()) {
+    std::vector<int32_t> f, n;
+    std::vector<int64_t> off;
+    std::vector<double> Vs;
+    for (const auto& b : e->eigen) {
+      f.push_back(b.first);
+      n.push_back(b.n);
+      off.push_back((int64_t)Vs.size());
+      Vs.insert(Vs.end(), b.V.begin(), b.V.end());
+    }
+    v.n_eigen = (int)e->eigen.size();
+    if ((rc = upload(f.data(), sizeof(int32_t) * f.size(), &p))) return rc;
+    v.eig_first = (const int32_t*)p;
+    if ((rc = upload(n.data(), sizeof(int32_t) * n.size(), &p))) return rc;
+    v.eig_n = (const int32_t*)p;
+    if ((rc = upload(off.data(), sizeof(int64_t) * off.size(), &p))) return rc;
+    v.eig_off = (const int64_t*)p;
+    if ((rc = upload(Vs.data(), sizeof(double) * Vs.size(), &p))) return rc;
+    v.eig_V = (const double*)p;
   }
   if ((rc = upload(e->data.data(), sizeof(double) * B, &p))) return rc;
   v.data = (const double*)p;

@@ -42,6 +42,13 @@ struct DevView {
   const double* mirror_hi;    // [n_params]
   const double* prior_mean;   // [n_params]
   const double* prior_icov;   // [n_params * n_params]
+  // eigen-decomposed parameter blocks: original[first + i] =
+  // sum_j V[i][j] * given[first + j] (V row-major n x n, at eig_V + eig_off)
+  int n_eigen;
+  const int32_t* eig_first;
+  const int32_t* eig_n;
+  const int64_t* eig_off;
+  const double* eig_V;
   const double* data;         // [n_bins]
   const TableDesc* tables;
   const TableFn* table_fns;

@@ -28,14 +28,33 @@ namespace {
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) k_params(const DevView v, const double* __restrict__ params) {
-  extern __shared__ double sp[];  // raw parameter vector of point k
+  extern __shared__ double sp[];  // raw parameter vector of point k [, original values]
   const int k = blockIdx.x;
   const int P = v.n_params;
   for (int p = threadIdx.x; p < P; p += blockDim.x) sp[p] = params[(size_t)k * P + p];
   __syncthreads();
+  // eigen-decomposed blocks back to the original parameters
+  // (ParameterSet::propagateEigenToOriginal, ParameterSet.cpp:766-780)
+  const double* so = sp;
+  if (v.n_eigen > 0) {
+    double* orig = sp + P;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) orig[p] = sp[p];
+    __syncthreads();
+    for (int b = 0; b < v.n_eigen; ++b) {
+      const int f = v.eig_first[b], n = v.eig_n[b];
+      const double* V = v.eig_V + v.eig_off[b];
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc = fma(V[(size_t)i * n + j], sp[f + j], acc);
+        orig[f + i] = acc;
+      }
+    }
+    __syncthreads();
+    so = orig;
+  }
   T* xs = (T*)v.x;
   for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    double x = sp[p];
+    double x = so[p];
     const double lo = v.mirror_lo[p], hi = v.mirror_hi[p];
     if (lo > -DBL_MAX && hi < DBL_MAX) {
       // DialInputBuffer.cpp:56-70
@@ -50,7 +69,9 @@ __global__ void __launch_bounds__(256) k_params(const DevView v, const double* _
     xs[(size_t)p * v.kpad + k] = (T)x;
   }
   if (!v.has_prior) return;
-  // delta^T C^-1 delta with u = C^-1 delta formed row by row.
+  // delta^T C^-1 delta on the parameters as given (the eigen parameters of
+  // decomposed blocks, as the reference's penalty in eigen mode), u = C^-1
+  // delta formed row by row.
   double acc = 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
     const double* row = v.prior_icov + (size_t)i * P;
@@ -228,7 +249,7 @@ __device__ __forceinline__ void named_arrive(int id, int count) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPlainThreads) k_plain_ws(const DevView v) {
+__global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain_ws(const DevView v) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
   T* dval = (T*)(smem + 2 * TB);                          // [2][1024]
@@ -252,16 +273,28 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain_ws(const DevView v) {
   __syncthreads();
 
   if (tid < kWsEval) {
+    // software pipeline of the per-tile loads: the headers of tile it + 1 are
+    // loaded at the end of iteration it from the descriptor fields loaded
+    // during iteration it - 1, so no global load sits on a tile's critical
+    // path (the evaluators need only the first dial and the dial count)
+    int nd = 0, d0 = 0, nd_next = 0, d0_next = 0;
+    if (ntile > 0) {
+      nd = v.tiles[blockIdx.x].ndials;
+      d0 = (int)v.tiles[blockIdx.x].dial0;
+    }
+    uint64_t h[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const int i = tid + j * kWsEval;
+      h[j] = (i < nd) ? v.hdr[d0 + i] : 0ull;
+    }
+    if (ntile > 1) {
+      nd_next = v.tiles[blockIdx.x + gridDim.x].ndials;
+      d0_next = (int)v.tiles[blockIdx.x + gridDim.x].dial0;
+    }
     for (int it = 0; it < ntile; ++it) {
       const int tile = blockIdx.x + it * gridDim.x;
       const int st = it & 1;
-      const TileDesc td = v.tiles[tile];
-      uint64_t h[6];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        const int i = tid + j * kWsEval;
-        h[j] = (i < td.ndials) ? v.hdr[td.dial0 + i] : 0ull;
-      }
       const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)((it >> 1) & 1), kWaitLimitNs);
       if (!ok) s_fail = 1;
       if (it >= 2) named_sync(kBarEmpty + st, kPlainThreads);  // the reducers are done with buffer st
@@ -271,7 +304,7 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain_ws(const DevView v) {
 #pragma unroll
         for (int j = 0; j < 6; ++j) {
           const int i = tid + j * kWsEval;
-          if (i < td.ndials) {
+          if (i < nd) {
             T val[1];
             dial_values<T, 1>(v, h[j], pl, 0, 0, val);
             dv[hdr_slot(h[j])] = val[0];
@@ -279,6 +312,19 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain_ws(const DevView v) {
         }
       }
       named_arrive(kBarFull + st, kPlainThreads);
+      if (it + 1 < ntile) {
+        nd = nd_next;
+        d0 = d0_next;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+          const int i = tid + j * kWsEval;
+          h[j] = (i < nd) ? v.hdr[d0 + i] : 0ull;
+        }
+        if (it + 2 < ntile) {
+          nd_next = v.tiles[tile + 2 * gridDim.x].ndials;
+          d0_next = (int)v.tiles[tile + 2 * gridDim.x].dial0;
+        }
+      }
       named_sync(kBarEval, kWsEval);  // stage st fully read
       if (tid == 0 && it + 2 < ntile) issue_tile(v, tile + 2 * gridDim.x, smem + st * TB, &bar[st]);
     }
@@ -490,14 +536,16 @@ int batched_blocks_per_sm(const DevView& v, const BatchedShape& b) {
   return n;
 }
 
+size_t params_smem_bytes(const DevView& v) { return (size_t)v.n_params * sizeof(double) * (v.n_eigen > 0 ? 2 : 1); }
+
 cudaError_t prepare_params(const DevView& v) {
-  const size_t smem = (size_t)v.n_params * sizeof(double);
+  const size_t smem = params_smem_bytes(v);
   const void* fn = v.precision ? (const void*)k_params<float> : (const void*)k_params<double>;
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s) {
-  const size_t smem = (size_t)v.n_params * sizeof(double);
+  const size_t smem = params_smem_bytes(v);
   if (v.precision)
     k_params<float><<<K, 256, smem, s>>>(v, params);
   else

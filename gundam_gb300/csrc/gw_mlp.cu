@@ -567,21 +567,22 @@ __global__ void __launch_bounds__(256) k_head_llh(Head h, const float* __restric
     racc[j] = bin_ok ? h.r_b[bin] : 0.f;
   }
   if (bin_ok) {
-    const float* tab = h.tab + bin;
-    const float* rw = h.r_w ? h.r_w + bin : nullptr;
+    const float* __restrict__ tab = h.tab + bin;
+    const float* __restrict__ rw = h.r_w ? h.r_w + bin : nullptr;
     const int nb = h.nb;
+#pragma unroll 4
     for (int k = 0; k < din; ++k) {
-      const float w = rw ? rw[(size_t)k * nb] : 0.f;
+      const float w = rw ? __ldg(rw + (size_t)k * nb) : 0.f;
 #pragma unroll
       for (int j = 0; j < PPT; ++j) {
         const int e = (threadIdx.y + 8 * j) * din + k;
         const int off = s_off[e];
         const float t = s_t[e];
         if (additive) {
-          const float lo = tab[off], hi = tab[off + nb];
+          const float lo = __ldg(tab + off), hi = __ldg(tab + off + nb);
           acc[j] += fmaf(t, hi - lo, lo);
         } else {
-          acc[j] = fmaf(t, tab[off], acc[j]);
+          acc[j] = fmaf(t, __ldg(tab + off), acc[j]);
         }
         racc[j] = fmaf(s_z[e], w, racc[j]);
       }

@@ -209,7 +209,12 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
     sig_p, sig_d = xp.std(0), xd.std(0)
     mean_diff = np.abs(xd.mean(0) - xp.mean(0))
     se = np.sqrt(sig_p ** 2 / ess_p + sig_d ** 2 / ess_d)
+    worst_d = np.argsort(ess_d)[:8]
+    worst_p = np.argsort(ess_p)[:8]
     res = {
+        "slowest_parameters": {"delayed": [[int(i), float(ess_d[i]), float(ess_p[i])] for i in worst_d],
+                               "plain": [[int(i), float(ess_p[i]), float(ess_d[i])] for i in worst_p],
+                               "columns": "parameter, ESS of this sampler, ESS of the other"},
         "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {B} bins, {P} params",
         "precision": precision, "chains": chains, "plain_steps": steps, "delayed_steps": da_steps, "n_sub": n_sub,
         "thin": thin, "warm_steps": warm_steps, "warm_seconds": t_warm, "burn_fraction": burn_frac,

@@ -122,6 +122,11 @@ class Engine:
         m, ic = _c(mean, np.float64), _c(icov, np.float64)
         self._chk(self.lib.gw_set_prior(self._e, _ptr(m), _ptr(ic)))
 
+    def add_eigen_block(self, first, V):
+        V = _c(V, np.float64)
+        self._keep.append(V)
+        self._chk(self.lib.gw_add_eigen_block(self._e, int(first), V.shape[0], _ptr(V)))
+
     def initialize(self): self._chk(self.lib.gw_initialize(self._e))
 
     # ---- evaluation ----

@@ -186,6 +186,15 @@ int gw_set_likelihood(gw_engine* e, int32_t llh_type);
  * inv_cov is n_params*n_params row-major; NULL clears the prior. */
 int gw_set_prior(gw_engine* e, const double* mean, const double* inv_cov);
 
+/* Eigen-decomposed parameter set (ParameterSet::propagateEigenToOriginal,
+ * ParameterSet.cpp:766-780; ParametersManager::convertEigenToOrig,
+ * ParametersManager.cpp:329-334): parameters [first, first + n) passed to
+ * gw_eval are eigen parameters, and the engine forms the original ones as
+ * V * given (V [n x n] row-major, columns = eigenvectors) on the device before
+ * mirroring and the dials.  The prior penalty applies to the parameters as
+ * passed (the reference's eigen-mode penalty).  Blocks may not overlap. */
+int gw_add_eigen_block(gw_engine* e, int32_t first, int32_t n, const double* V);
+
 /* Packs, sorts, validates and uploads everything (RecursiveSums::Initialize,
  * CacheRecursiveSums.cpp:92-153, plus the hemi uploads).  After this the
  * builder calls above return GW_ERR_STATE. */

@@ -124,3 +124,25 @@ def test_bad_config_rejected():
     p = C.c_void_p()
     assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
     assert "bad gw_config" in N.last_error(None)
+
+
+def test_eigen_block_validation():
+    """gw_add_eigen_block refuses blocks outside the parameters, overlapping
+    blocks and non-finite matrices (before any device work)."""
+    import ctypes as C
+    import numpy as np
+    from gundam_gb300 import _native as N
+    lib = N.libgw()
+    cfg = N.GwConfig(10, 6, 4, 1, N.GW_FP64, 0, 0, 0)
+    e = C.c_void_p()
+    assert lib.gw_create(C.byref(cfg), C.byref(e)) == N.GW_OK
+    V = np.eye(3)
+    p = V.ctypes.data_as(C.c_void_p)
+    assert lib.gw_add_eigen_block(e, 4, 3, p) == N.GW_ERR_ARG      # [4, 7) beyond 6 parameters
+    assert lib.gw_add_eigen_block(e, 0, 3, p) == N.GW_OK
+    assert lib.gw_add_eigen_block(e, 2, 3, p) == N.GW_ERR_ARG      # overlaps [0, 3)
+    bad = np.eye(3)
+    bad[1, 1] = np.nan
+    assert lib.gw_add_eigen_block(e, 3, 3, bad.ctypes.data_as(C.c_void_p)) == N.GW_ERR_NOT_FINITE
+    assert lib.gw_add_eigen_block(e, 3, 3, p) == N.GW_OK
+    lib.gw_destroy(e)

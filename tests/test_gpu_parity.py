@@ -360,3 +360,24 @@ def test_both_k1_kernels_agree_bit_for_bit(mixed, prec):
     r = eng.eval(pt)
     np.testing.assert_array_equal(r[0], out[0][0])
     eng.close()
+
+
+def test_eigen_decomposed_parameters(c1, c1_oracle):
+    """Parameters given in the eigen basis of the prior covariance (original =
+    V * eigen on the device) reproduce the oracle at the original values; a
+    diagonal prior on the eigen parameters gives the original penalty."""
+    lam, V = np.linalg.eigh(c1.prior_cov)
+    # the cache with one eigen block over all parameters and the eigen-space prior
+    e2 = Engine.from_workload(c1, precision="fp64", k_max=8, prior=False, initialize=False)
+    e2.add_eigen_block(0, V)
+    e2.set_prior(V.T @ c1.prior_mean, np.diag(1.0 / lam))
+    e2.initialize()
+    x = c1.draw_points(8, 91)
+    y = x @ V  # eigen = V^T x, row-wise
+    s, s2, llh, stat = e2.eval(y)
+    r = c1_oracle.eval(x)
+    np.testing.assert_allclose(s, r["sums"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(s2, r["sums2"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(stat, r["llh_stat"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(llh, r["llh"], rtol=1e-10, atol=1e-6)
+    e2.close()
