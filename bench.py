@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--mcmc-train", type=int, default=65536)
     ap.add_argument("--mcmc-epochs", type=int, default=50)
     ap.add_argument("--mcmc-nsub", type=int, default=40)
+    ap.add_argument("--mcmc-stage1", default="hmc", choices=["hmc", "rwm"])
     return ap.parse_args()
 
 
@@ -271,14 +272,17 @@ def c3_sweep(local, steps=20, warmup=3):
 
 def mcmc_comparison(args):
     """ESS/s of the surrogate delayed-acceptance sampler against the plain
-    engine sampler on this GPU (64 chains, the same proposal and start
-    states, the same number of steps), with a short training of the
-    surrogate; see gundam_gb300/da_mcmc.py."""
+    engine sampler on this GPU (64 chains, the same start states, the same
+    number of steps; the plain sampler's random walk uses the adaptive
+    pilot's proposal), with a short training of the surrogate.  Stage 1 is
+    Hamiltonian Monte Carlo on the surrogate (its device gradient) by
+    default, random-walk sub-chains with --mcmc-stage1 rwm; the exact engine
+    corrects every stage-1 proposal.  See gundam_gb300/da_mcmc.py."""
     from gundam_gb300 import da_mcmc
 
     r = da_mcmc.run(events=args.events, train=args.mcmc_train, epochs=args.mcmc_epochs, steps=args.mcmc_steps,
                     n_sub=args.mcmc_nsub, seed=args.seed, config=args.config, precision=args.precision,
-                    linear=False, lr=2e-3, thin=2)
+                    linear=False, lr=2e-3, thin=2, stage1=args.mcmc_stage1)
     p, d = r["plain"], r["delayed"]
     return {
         "metric": "ESS/s, surrogate delayed acceptance vs plain engine MCMC (same GPU)",
@@ -288,7 +292,7 @@ def mcmc_comparison(args):
         "gain": {"min": r["ess_per_s_gain_min"], "median": r["ess_per_s_gain_median"]},
         "stage2_accept": d["stage2_accept"], "plain_accept": p["accept"], "fell_back_at_step": d["fell_back_at_step"],
         "surrogate_llh_error_sd": r["surrogate_llh_error_sd"], "posterior": r["posterior"],
-        "chains": r["chains"], "steps_each": r["plain_steps"], "n_sub": r["n_sub"],
+        "chains": r["chains"], "steps_each": r["plain_steps"], "stage1": r["stage1"],
         "seconds": {"plain": p["seconds"], "delayed": d["seconds"], "pilot": r["pilot"]["seconds"],
                     "training_data": r["training"]["data_seconds"], "training": r["training"]["train_seconds"],
                     "total": r["total_seconds"]},

@@ -177,6 +177,7 @@ GW_SIGNATURES: dict[str, list] = {
     "gwm_set_head_additive": [_P, _P, _P, _I32, C.c_float, _P, _P, _P, _P, _P, _P, _P],
     "gwm_set_chain": [_P, _P, _P, _P],
     "gwm_substeps": [_P, _P, _P, _I32, _I32, _I32, C.c_uint64, _P, _P, _P],
+    "gwm_value_grad": [_P, _P, _I32, _I32, _P, _P],
     "gwm_train_reserve": [_P, C.c_int64],
     "gwm_train_size": [_P, _P],
     "gwm_train_append": [_P, _P, _P, _I32, _I32],

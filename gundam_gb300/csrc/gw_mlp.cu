@@ -518,6 +518,38 @@ __device__ __forceinline__ float llh_term_f(int type, float data, float pred, fl
   return 2.f * stat + 2.f * penalty;
 }
 
+// Derivatives of the FP32 per-bin term with respect to log(rate) and to
+// log(sum w^2):
+//   Poisson: dL/dlog mu = 2 (mu - n), dL/dlog s2 = 0;
+//   Barlow-Beeston OA2021: beta minimises the bin's joint likelihood (its
+//   quadratic is the stationarity condition), so by the envelope theorem the
+//   derivatives are the partials at fixed beta of
+//   L = 2 (beta mu - n + n log(n / (beta mu))) + (beta - 1)^2 mu^2 / s2:
+//     dL/dlog mu = 2 (beta mu - n) + 2 (beta - 1)^2 / f2,
+//     dL/dlog s2 = -(beta - 1)^2 / f2,  f2 = s2 / mu^2.
+__device__ __forceinline__ void llh_term_grad_f(int type, float data, float pred, float sumw2, float& gmu,
+                                                float& gs2) {
+  gmu = 0.f;
+  gs2 = 0.f;
+  if (type == GW_LLH_POISSON) {
+    if (pred > 0.f) gmu = 2.f * (pred - data);
+    return;
+  }
+  if (type != GW_LLH_BARLOW_BEESTON_OA2021 || !(pred > 0.f)) return;
+  if (sumw2 > 0.f) {
+    const float f2 = sumw2 / (pred * pred);
+    const float temp = sumw2 / pred - 1.f;
+    const float temp2 = temp * temp + 4.f * data * f2;
+    if (temp2 < 0.f) return;
+    const float beta = 0.5f * (sqrtf(temp2) - temp);
+    const float pen = (beta - 1.f) * (beta - 1.f) / f2;
+    gmu = 2.f * (beta * pred - data) + 2.f * pen;
+    gs2 = -pen;
+  } else {
+    gmu = 2.f * (pred - data);
+  }
+}
+
 // Head and likelihood terms, fused.  Block (32 bins, 8 point rows); thread
 // (x, y) of block (bx, by) handles bin 32 bx + x and the PPT points
 // by * 8 PPT + y + 8 j.  The block first stages, for each of its points and
@@ -527,11 +559,16 @@ __device__ __forceinline__ float llh_term_f(int type, float data, float pred, fl
 // the table lines of a bin shared through L1 across the block's points.
 // Per point and block, the 32 bins' terms are summed by a fixed shuffle tree
 // into part[point][bx] (FP64); optional outputs: sums, sums2 (FP64), log rates.
-template <int PPT>
+// GRAD: also, per (point, bin), G = dL/dlog mu + dL/dlog s2 (the derivative
+// with respect to the log rate, the modelled sum of w^2 moving with it) and
+// S = dL/dlog s2 into gbuf / sbuf, and dY = G * sd (the derivative with
+// respect to the network output) as BF16 into dy.
+template <int PPT, bool GRAD = false>
 __global__ void __launch_bounds__(256) k_head_llh(Head h, const float* __restrict__ x, const float* __restrict__ mlp,
                                                   int C, const double* __restrict__ data, int llh_type,
                                                   double* __restrict__ part, double* sums, double* sums2,
-                                                  double* logr) {
+                                                  double* logr, float* gbuf = nullptr, float* sbuf = nullptr,
+                                                  bf16* dy = nullptr) {
   extern __shared__ unsigned char sh_raw[];
   constexpr int NP = 8 * PPT;  // points per block
   const int din = h.din;
@@ -600,6 +637,14 @@ __global__ void __launch_bounds__(256) k_head_llh(Head h, const float* __restric
       if (sums) sums[o] = (double)mu;
       if (sums2) sums2[o] = (double)s2;
       if (logr) logr[o] = (double)lr;
+      if constexpr (GRAD) {
+        float gmu, gs2;
+        llh_term_grad_f(llh_type, (float)data[bin], mu, s2, gmu, gs2);
+        const float G = gmu + gs2;
+        gbuf[o] = G;
+        sbuf[o] = gs2;
+        dy[o] = __float2bfloat16(G * h.sd[bin]);
+      }
     }
     double t = (double)term;
     for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
@@ -616,6 +661,119 @@ __global__ void k_llh_finish(const double* __restrict__ part, int nblk, int C, d
   for (int b = lane; b < nblk; b += 32) s += part[(size_t)m * nblk + b];
   for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   if (lane == 0) llh[m] = s;
+}
+
+// Gradient of the likelihood through the base and the sum-of-w^2 model, for
+// point m = blockIdx.x and parameters k = blockIdx.y * 8 + (0..7):
+//   gz[m][k] = sum_b G[m][b] * d base_b / d x_k + S[m][b] * r_w[k][b]
+// (d base / d x_k: the slope of the interpolation interval of x_k, zero
+// outside [-lim, lim]; affine base: tab[k][b]).  The point's G and S rows are
+// staged in shared memory; fixed-order block reduction.
+__global__ void __launch_bounds__(256) k_base_grad(Head h, const float* __restrict__ x, const float* __restrict__ G,
+                                                   const float* __restrict__ S, float* __restrict__ gz) {
+  extern __shared__ float shg[];
+  float* g = shg;            // [nb]
+  float* sg = shg + h.nb;    // [nb]
+  __shared__ float red[8][8];
+  const int m = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int b = tid; b < h.nb; b += 256) {
+    g[b] = G[(size_t)m * h.nb + b];
+    sg[b] = S[(size_t)m * h.nb + b];
+  }
+  __syncthreads();
+  const bool additive = h.nodes >= 2;
+  const float inv_w = additive ? (float)(h.nodes - 1) / (2.f * h.lim) : 0.f;
+  for (int q = 0; q < 8; ++q) {
+    const int k = blockIdx.y * 8 + q;
+    if (k >= h.din) break;
+    const float z = x[(size_t)m * h.din + k];
+    const float* lo;
+    float scale_ = 1.f;
+    if (additive) {
+      const float xc = fminf(fmaxf(z, -h.lim), h.lim);
+      const float u = (xc + h.lim) * inv_w;
+      const int i = min((int)u, h.nodes - 2);
+      lo = h.tab + ((size_t)k * h.nodes + i) * h.nb;
+      scale_ = (z > -h.lim && z < h.lim) ? inv_w : 0.f;
+    } else {
+      lo = h.tab + (size_t)k * h.nb;
+    }
+    const float* rw = h.r_w ? h.r_w + (size_t)k * h.nb : nullptr;
+    float acc = 0.f;
+    for (int b = tid; b < h.nb; b += 256) {
+      const float slope = additive ? (lo[b + h.nb] - lo[b]) * scale_ : lo[b];
+      acc = fmaf(g[b], slope, acc);
+      if (rw) acc = fmaf(sg[b], rw[b], acc);
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[q][warp] = acc;
+  }
+  __syncthreads();
+  if (tid < 8) {
+    const int k = blockIdx.y * 8 + tid;
+    if (k < h.din) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[tid][w];
+      gz[(size_t)m * h.din + k] = t;
+    }
+  }
+}
+
+// Per point (block), G groups of P32 threads as k_finish_accept: the value
+// f = llh + penalty and the gradient with respect to the parameters,
+// (gz + dx) / scale + 2 C^-1 (theta - mean) (prior optional).
+__global__ void k_grad_finish(const double* __restrict__ part, int nblk, const double* __restrict__ theta, int P,
+                              const float* __restrict__ scale, const float* __restrict__ gz,
+                              const float* __restrict__ dx, const double* __restrict__ m,
+                              const float* __restrict__ icov, double* __restrict__ f, double* __restrict__ grad) {
+  extern __shared__ float shf2[];
+  const int P32 = (P + 31) & ~31, Gn = blockDim.x / P32;
+  float* d = shf2;              // [P32]
+  float* up = shf2 + P32;       // [Gn][P32]
+  float* red = up + Gn * P32;   // [P32]
+  __shared__ double s_llh;
+  const int c = blockIdx.x, lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int b = lane; b < nblk; b += 32) t += part[(size_t)c * nblk + b];
+    for (int off = 16; off; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0) s_llh = t;
+  }
+  const int g = threadIdx.x / P32, p = threadIdx.x - g * P32;
+  if (m) {
+    if (g == 0) d[p] = p < P ? (float)(theta[(size_t)c * P + p] - m[p]) : 0.f;
+    __syncthreads();
+    const int ks = (P + Gn - 1) / Gn;
+    if (p < P) {
+      const int k0 = g * ks, k1 = min(P, (g + 1) * ks);
+      float u0 = 0.f, u1 = 0.f;
+      int k = k0;
+      for (; k + 2 <= k1; k += 2) {
+        u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+        u1 = fmaf(icov[(size_t)(k + 1) * P + p], d[k + 1], u1);
+      }
+      for (; k < k1; ++k) u0 = fmaf(icov[(size_t)k * P + p], d[k], u0);
+      up[g * P32 + p] = u0 + u1;
+    }
+    __syncthreads();
+  }
+  if (g == 0) {
+    float u = 0.f;
+    if (m)
+      for (int q = 0; q < Gn; ++q) u += (p < P) ? up[q * P32 + p] : 0.f;
+    red[p] = m ? d[p] * u : 0.f;
+    if (p < P) {
+      const size_t o = (size_t)c * P + p;
+      grad[o] = (double)((gz[o] + dx[o]) / scale[p]) + (m ? 2.0 * (double)u : 0.0);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double pen = 0.0;
+    if (m)
+      for (int i = 0; i < P32; ++i) pen += (double)red[i];
+    f[c] = s_llh + pen;
+  }
 }
 
 // Training target of a reweighted point, one thread per (point, bin):
@@ -674,6 +832,9 @@ struct gwm_net {
         *h_rb = nullptr, *h_rw = nullptr;
   double *h_data = nullptr, *h_theta = nullptr, *h_sums = nullptr, *h_sums2 = nullptr, *h_llh = nullptr,
          *h_logr = nullptr, *h_part = nullptr;
+  // gradient buffers (gwm_value_grad), allocated on first use
+  float *g_G = nullptr, *g_S = nullptr, *g_gz = nullptr, *g_dx = nullptr;
+  double *g_f = nullptr, *g_grad = nullptr;
   // training set on the device (gwm_train_reserve / gwm_train_append*):
   // standardised inputs [train_max x dims[0]] and targets [train_max x dims[L]]
   float *train_x = nullptr, *train_t = nullptr;
@@ -1687,5 +1848,86 @@ extern "C" int gwm_substeps(gwm_net* n, const double* theta0, const double* f0, 
   GWM_CUDA(n, cudaMemcpyAsync(phi, s->phi, sizeof(double) * (size_t)C * P, cudaMemcpyDeviceToHost, n->stream));
   GWM_CUDA(n, cudaMemcpyAsync(fphi, s->f, sizeof(double) * C, cudaMemcpyDeviceToHost, n->stream));
   if (n_acc) GWM_CUDA(n, cudaMemcpyAsync(n_acc, s->nacc, sizeof(int32_t) * C, cudaMemcpyDeviceToHost, n->stream));
+  return check_status(n);
+}
+
+// ---------------------------------------------------------------------------
+// Gradient of the surrogate -2 log L (plus the chain's prior penalty, when
+// gwm_set_chain gave one) with respect to the parameters.
+// ---------------------------------------------------------------------------
+// dX of the network for dY in dz[L-1]: the backward GEMMs without the weight
+// gradients; the input gradient lands in g_dx (FP32).
+static int backward_dx(gwm_net* n, int B) {
+  const int L = n->n_layers;
+  for (int l = L - 1; l >= 1; --l) {
+    gwm::Epilogue e{};
+    e.gate = n->z[l - 1];
+    e.out_bf16 = n->dz[l - 1];
+    int rc = gemm(n, n->dz[l], n->wt[l], B, n->dims[l], n->dims[l + 1], e);
+    if (rc) return rc;
+  }
+  gwm::Epilogue e0{};
+  e0.out_f32 = n->g_dx;
+  return gemm(n, n->dz[0], n->wt[0], B, n->dims[0], n->dims[1], e0);
+}
+
+extern "C" int gwm_value_grad(gwm_net* n, const double* theta, int32_t C, int32_t llh_type, double* f, double* grad) {
+  if (!n || !theta || !f || !grad || C < 1 || C > n->batch_max) return gwm_fail(n, GW_ERR_ARG, "gwm_value_grad: bad batch");
+  if (!n->has_head) return gwm_fail(n, GW_ERR_STATE, "gwm_value_grad: gwm_set_head first");
+  if (n->dims[0] > 1024) return gwm_fail(n, GW_ERR_LIMIT, "gwm_value_grad: at most 1024 parameters");
+  GWM_CUDA(n, cudaSetDevice(n->device));
+  const int din = n->dims[0], nb = n->dims[n->n_layers], L = n->n_layers, Bm = n->batch_max;
+  const int Bp = ((C + 7) / 8) * 8;
+  if (Bp > Bm) return gwm_fail(n, GW_ERR_ARG, "gwm_value_grad: batch above batch_max after padding");
+  if (!n->g_G) {
+    int rc = gwm_alloc(n, &n->g_G, (size_t)Bm * nb) | gwm_alloc(n, &n->g_S, (size_t)Bm * nb) |
+             gwm_alloc(n, &n->g_gz, (size_t)Bm * din) | gwm_alloc(n, &n->g_dx, (size_t)Bm * din) |
+             gwm_alloc(n, &n->g_f, Bm) | gwm_alloc(n, &n->g_grad, (size_t)Bm * din);
+    if (rc) return rc;
+  }
+  if (Bp > C) GWM_CUDA(n, cudaMemsetAsync(n->h_theta, 0, sizeof(double) * (size_t)Bp * din, n->stream));
+  GWM_CUDA(n, cudaMemcpyAsync(n->h_theta, theta, sizeof(double) * (size_t)C * din, cudaMemcpyHostToDevice, n->stream));
+  gwm::k_standardize<<<(unsigned)(((size_t)Bp * din + 255) / 256), 256, 0, n->stream>>>(n->h_theta, Bp, din,
+                                                                                     n->h_mean, n->h_scale, n->xin);
+  int rc = stage_input(n, n->xin, nullptr, Bp, false);
+  if (!rc) rc = forward(n, Bp);
+  if (rc) return rc;
+  // the head: likelihood partials, G, S and dY (rows C..Bp of dY stay zero)
+  GWM_CUDA(n, cudaMemsetAsync(n->dz[L - 1], 0, sizeof(bf16) * (size_t)Bp * nb, n->stream));
+  constexpr int kPPT = 2;
+  const int nbx = (nb + 31) / 32;
+  const size_t shm = (size_t)8 * kPPT * din * 12;
+  if (shm > 48 * 1024) {
+    static std::once_flag once;
+    std::call_once(once, []() {
+      cudaFuncSetAttribute(gwm::k_head_llh<kPPT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (shm > 200 * 1024) return gwm_fail(n, GW_ERR_LIMIT, "surrogate head: too many inputs");
+  }
+  gwm::k_head_llh<kPPT, true><<<dim3(nbx, (C + 8 * kPPT - 1) / (8 * kPPT)), dim3(32, 8), shm, n->stream>>>(
+      head_view(n), n->xin, n->z[L - 1], C, n->h_data, llh_type, n->h_part, nullptr, nullptr, nullptr, n->g_G,
+      n->g_S, n->dz[L - 1]);
+  GWM_CUDA(n, cudaGetLastError());
+  rc = backward_dx(n, Bp);
+  if (rc) return rc;
+  const size_t shb = sizeof(float) * 2 * (size_t)nb;
+  if (shb > 48 * 1024) {
+    if (shb > 200 * 1024) return gwm_fail(n, GW_ERR_LIMIT, "gwm_value_grad: too many bins");
+    static std::once_flag once2;
+    std::call_once(once2, []() {
+      cudaFuncSetAttribute(gwm::k_base_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+  }
+  gwm::k_base_grad<<<dim3(C, (din + 7) / 8), 256, shb, n->stream>>>(head_view(n), n->xin, n->g_G, n->g_S, n->g_gz);
+  GWM_CUDA(n, cudaGetLastError());
+  const int P32 = (din + 31) & ~31;
+  const int Gn = std::max(1, std::min(4, 1024 / P32));
+  const bool prior = n->chain && n->chain->prior;
+  gwm::k_grad_finish<<<C, (unsigned)(Gn * P32), sizeof(float) * (size_t)P32 * (Gn + 2), n->stream>>>(
+      n->h_part, nbx, n->h_theta, din, n->h_scale, n->g_gz, n->g_dx, prior ? n->chain->m : nullptr,
+      prior ? n->chain->icov : nullptr, n->g_f, n->g_grad);
+  GWM_CUDA(n, cudaGetLastError());
+  GWM_CUDA(n, cudaMemcpyAsync(f, n->g_f, sizeof(double) * C, cudaMemcpyDeviceToHost, n->stream));
+  GWM_CUDA(n, cudaMemcpyAsync(grad, n->g_grad, sizeof(double) * (size_t)C * din, cudaMemcpyDeviceToHost, n->stream));
   return check_status(n);
 }

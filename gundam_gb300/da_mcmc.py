@@ -65,7 +65,7 @@ def _sampler_stats(ch, seconds, burn):
 def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=2, config="c2", log=None,
         precision="fp32", region="posterior", proposal="adapted", base_points=32768, nodes=8, batch=2048,
         lr=1e-3, linear=True, max_error=20.0, adapt_cycles=6, adapt_steps=200, da_steps=None, thin=1,
-        warm_steps=500, burn_frac=0.1):
+        warm_steps=500, burn_frac=0.1, stage1="hmc", eps=0.25, n_leap=10):
     """Fit, adapt, train, then sample with both samplers from the same states
     (``steps`` plain steps and ``da_steps`` (default: the same) delayed steps)."""
     log = log or (lambda *_: None)
@@ -179,12 +179,20 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
         sur.substeps(th0, None, n_sub, r)
     t_sub = (time.perf_counter() - t0) / 5
     t0 = time.perf_counter()
+    for r in range(5):
+        sur.value_grad(th0)
+    t_grad = (time.perf_counter() - t0) / 5
+    t0 = time.perf_counter()
     for _ in range(5):
         f_exact(th0)
     t_exact = (time.perf_counter() - t0) / 5
 
     # 4. sampling, both samplers from the same states with the same proposal
+    L_post = np.linalg.cholesky(cov_post)
+
     def stage1_of(su):
+        if stage1 == "hmc":
+            return mcmc.hmc_stage1(su.value_grad, L_post, eps=eps, n_leap=n_leap)
         return lambda th, fs, ns, sd: su.substeps(th, fs, ns, sd)
     # both samplers start from the same states, taken after a delayed-
     # acceptance warm-up (it mixes fastest) so that neither starts out of
@@ -226,7 +234,10 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
                      "base_points": n_b, "base_data_seconds": t_base_data, "base_fit_seconds": t_base_fit,
                      "data_seconds": t_data, "train_seconds": t_train, "loss_first_last": [hist[0], hist[-1]]},
         "surrogate_llh_error_sd": err,
-        "seconds_per_step": {"surrogate_substeps": t_sub, "exact": t_exact, "points": chains},
+        "seconds_per_step": {"surrogate_substeps": t_sub, "surrogate_value_grad": t_grad, "exact": t_exact,
+                             "points": chains},
+        "stage1": {"kind": stage1, "n_sub": n_sub} if stage1 == "rwm" else
+                  {"kind": "hmc", "eps": eps, "n_leap": n_leap, "mass": "posterior covariance from the pilot"},
         "plain": dict(st_p, accept=p["accept"], n_exact=p["n_exact"]),
         "delayed": dict(st_d, stage2_accept=d["stage2_accept"], accept=d["accept"], n_exact=d["n_exact"],
                         n_surrogate=d["n_surrogate"], fell_back_at_step=d["fell_back_at_step"],
@@ -272,6 +283,9 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--thin", type=int, default=1)
     ap.add_argument("--warm-steps", type=int, default=500)
+    ap.add_argument("--stage1", default="hmc", choices=["hmc", "rwm"])
+    ap.add_argument("--eps", type=float, default=0.25)
+    ap.add_argument("--n-leap", type=int, default=10)
     ap.add_argument("--no-linear", action="store_true")
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args()
@@ -279,7 +293,7 @@ def main():
     print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config,
                          precision=a.precision, region=a.region, proposal=a.proposal, nodes=a.nodes,
                          linear=not a.no_linear, log=lg, da_steps=a.da_steps or None, lr=a.lr, thin=a.thin,
-                         warm_steps=a.warm_steps)))
+                         warm_steps=a.warm_steps, stage1=a.stage1, eps=a.eps, n_leap=a.n_leap)))
 
 
 if __name__ == "__main__":

@@ -89,6 +89,54 @@ def adapt(f_exact, theta0, cov0, cycles=4, steps=150, seed=0, target=0.234, reco
             "chains": last if record_last else None}
 
 
+def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1):
+    """Stage 1 of delayed acceptance as Hamiltonian Monte Carlo on the
+    surrogate density exp(-f_s/2): returns a callable (theta, fs, n, seed) ->
+    (phi, f_s(phi), accepted) for ``delayed(stage1=...)``.
+
+    value_grad(theta [C x P]) -> (f_s [C], d f_s/d theta [C x P]).  Each of the
+    ``n_trans`` transitions draws momenta q ~ N(0, I), runs ``n_leap`` leapfrog
+    steps of U = f_s/2 with the mass matrix (L L^T)^-1 (x moves by eps L q, q by
+    eps L^T grad U), the step jittered per chain uniformly in [0.8, 1.2] x eps
+    independently of the state, and accepts with exp(H0 - H1).  Leapfrog with
+    any deterministic gradient field is a volume-preserving reversible map, so
+    each transition is reversible with respect to exp(-f_s/2) and the
+    delayed-acceptance correction keeps the exact posterior invariant.  The
+    ``n`` argument of the callable is ignored in favour of ``n_trans`` except
+    that n == 0 only evaluates f_s."""
+    L = np.asarray(L, dtype=np.float64)
+
+    def stage1(theta, fs, n, seed):
+        x = np.array(theta, dtype=np.float64)
+        C, P = x.shape
+        f, g = value_grad(x)
+        if n == 0:
+            return x, f, np.zeros(C, np.int32)
+        rng = np.random.default_rng(seed)
+        acc = np.zeros(C, np.int32)
+        for _ in range(n_trans):
+            q = rng.standard_normal((C, P))
+            e = eps * rng.uniform(0.8, 1.2, size=(C, 1))
+            u = rng.random(C)
+            h0 = 0.5 * f + 0.5 * np.sum(q * q, axis=1)
+            xn = x.copy()
+            qn = q - 0.5 * e * (0.5 * g) @ L
+            fn, gn = f, g
+            for step in range(n_leap):
+                xn = xn + e * (qn @ L.T)
+                fn, gn = value_grad(xn)
+                if step + 1 < n_leap:
+                    qn = qn - e * (0.5 * gn) @ L
+            qn = qn - 0.5 * e * (0.5 * gn) @ L
+            h1 = 0.5 * fn + 0.5 * np.sum(qn * qn, axis=1)
+            with np.errstate(over="ignore", invalid="ignore"):
+                a = np.log(np.maximum(u, 1e-300)) < (h0 - h1)
+            x[a], f[a], g[a] = xn[a], fn[a], gn[a]
+            acc += a
+        return x, f, acc
+    return stage1
+
+
 def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True, stage1=None,
             thin=1):
     """stage1: optional callable (theta, fs, n_sub, seed) -> (phi, fphi, n_acc)

@@ -371,6 +371,22 @@ class Surrogate:
              self.mlp._n)
         return phi, fphi, nacc
 
+    def value_grad(self, theta):
+        """(f_s, d f_s / d theta) at each point, on the device: the surrogate
+        -2 log L plus the prior penalty given to set_chain."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        f = np.empty(th.shape[0])
+        g = np.empty_like(th)
+        bm = self.mlp.batch_max
+        for s in range(0, th.shape[0], bm):
+            part = np.ascontiguousarray(th[s:s + bm])
+            fo = np.empty(part.shape[0])
+            go = np.empty_like(part)
+            _chk(N.libgw().gwm_value_grad(self.mlp._n, _p(part), part.shape[0], self.llh_type, _p(fo), _p(go)),
+                 self.mlp._n)
+            f[s:s + part.shape[0]], g[s:s + part.shape[0]] = fo, go
+        return f, g
+
     def linear_twin(self):
         """A surrogate with the same head (standardisation, base, output
         scaling, sum(w^2) model) and a network whose output is zero: the

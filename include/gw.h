@@ -376,6 +376,13 @@ int gwm_train_epochs(gwm_net* net, int32_t epochs, int32_t batch, float lr0, flo
 int gwm_set_chain(gwm_net* net, const double* prop_chol, const double* prior_mean, const double* prior_icov);
 int gwm_substeps(gwm_net* net, const double* theta0, const double* f0, int32_t C, int32_t n_sub, int32_t llh_type,
                  uint64_t seed, double* phi, double* fphi, int32_t* n_acc);
+/* Value and gradient of the surrogate -2 log L (plus the prior penalty of
+ * gwm_set_chain, when given) at C <= batch_max points theta [C x P] (host
+ * FP64): f [C], grad [C x P] (host).  The gradient runs back through the
+ * likelihood terms (closed-form derivatives), the base, the sum-of-w^2 model
+ * and the network (tcgen05 backward GEMMs).  A deterministic function of the
+ * point, so a leapfrog integrator built on it is exactly reversible. */
+int gwm_value_grad(gwm_net* net, const double* theta, int32_t C, int32_t llh_type, double* f, double* grad);
 /* The tensor-core GEMM alone: C [M x N] = A [M x K] * B [N x K]^T, BF16 in (raw bits), FP32 out, host arrays. */
 int gwm_gemm_test(const uint16_t* A, const uint16_t* B, int32_t M, int32_t N, int32_t K, float* C);
 

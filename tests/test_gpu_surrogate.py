@@ -302,3 +302,32 @@ def test_device_subchain_matches_host_replica(c2_small):
     assert np.allclose(phi, cur, rtol=0, atol=1e-6)
     assert np.allclose(fphi, fc, rtol=1e-6, atol=1e-4)
     assert acc.sum() > 0
+
+
+def test_value_grad_matches_finite_differences(c2_small):
+    """The device gradient of the surrogate -2 log L + prior penalty agrees
+    with central differences of the device value along random directions,
+    and the value equals the one the sub-chains use up to the penalty's
+    summation order."""
+    wl, eng, sur, th, sums = c2_small
+    P = wl.n_params
+    sur.set_chain(np.linalg.cholesky(1e-3 * wl.prior_cov), wl.prior_mean, wl.prior_icov)
+    pts = th[:4]
+    f, g = sur.value_grad(pts)
+    _, f_sub, _ = sur.substeps(pts, None, 0, 1)
+    np.testing.assert_allclose(f, f_sub, rtol=1e-6, atol=1e-3)
+    rng = np.random.default_rng(3)
+    h = 1e-3
+    rel = []
+    for _ in range(6):
+        v = rng.standard_normal((4, P))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        fp, _ = sur.value_grad(pts + h * v)
+        fm, _ = sur.value_grad(pts - h * v)
+        fd = (fp - fm) / (2 * h)
+        an = np.sum(g * v, axis=1)
+        rel.extend((np.abs(fd - an) / np.maximum(np.abs(an), 1.0)).tolist())
+    assert np.median(rel) < 0.03, rel
+    assert np.max(rel) < 0.2, rel
+    f2, g2 = sur.value_grad(pts)
+    assert np.array_equal(f, f2) and np.array_equal(g, g2)

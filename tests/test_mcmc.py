@@ -74,3 +74,33 @@ def test_ess_of_independent_draws_is_close_to_n():
     x = rng.standard_normal((4000, 4, 3))
     e = mcmc.ess(x)
     assert np.all(e > 0.8 * 16000) and np.all(e < 1.2 * 16000)
+
+
+def test_delayed_with_hmc_stage1_is_exact_with_a_biased_surrogate():
+    """Hamiltonian stage 1 on a wrong surrogate (shifted mean, wider
+    covariance) still samples the exact target after the stage-2 correction,
+    and with a good surrogate its proposals are far apart (large ESS per
+    exact evaluation)."""
+    mean, cov, icov, f = _target()
+    shift = 0.3 * np.sqrt(np.diag(cov))
+    icov_s = np.linalg.inv(1.3 * cov)
+
+    def vg_bad(th):
+        d = th - mean - shift
+        return np.einsum("ij,jk,ik->i", d, icov_s, d), 2.0 * d @ icov_s
+
+    Lc = np.linalg.cholesky(cov)
+    s1 = mcmc.hmc_stage1(vg_bad, Lc, eps=0.4, n_leap=6)
+    r = mcmc.delayed(f, None, np.tile(mean, (32, 1)), 1500, Lc, n_sub=1, seed=3, max_error=1e9, stage1=s1)
+    x = r["chains"][200:].reshape(-1, mean.size)
+    assert np.allclose(x.mean(0), mean, atol=0.1)
+    assert np.allclose(x.std(0), np.sqrt(np.diag(cov)), rtol=0.1)
+
+    def vg_good(th):
+        d = th - mean
+        return np.einsum("ij,jk,ik->i", d, icov, d), 2.0 * d @ icov
+    s2 = mcmc.hmc_stage1(vg_good, Lc, eps=0.4, n_leap=6)
+    d = mcmc.delayed(f, None, np.tile(mean, (32, 1)), 600, Lc, n_sub=1, seed=4, stage1=s2)
+    p = mcmc.plain(f, np.tile(mean, (32, 1)), 600, mcmc.proposal_chol(cov), seed=5)
+    assert d["stage2_accept"] > 0.99
+    assert mcmc.ess(d["chains"], burn=60).min() > 5 * mcmc.ess(p["chains"], burn=60).min()
