@@ -366,6 +366,9 @@ def run_gw(args, world, rank, local, dist):
             traffic = tr[key]
     layout = eng.layout()
     shape = eng.shape()
+    sidx = eng.shape_index()
+    sfull = Engine.compiled_shapes()[sidx] if sidx >= 0 else None
+    plain_name = ["k_plain", "k_plain_ws"][eng.plain_kernel()]
     variants = {}
     if not args.no_variants:
         # the same engine at K=1 (plain kernel), and the FP64 engine at K=1
@@ -374,6 +377,12 @@ def run_gw(args, world, rank, local, dist):
         variants[f"{args.precision}_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
             "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9}
+        if K > 16:
+            # C3 at the C2 size: K = 16 on this engine, K = 256 on one sized for it
+            eng.autotune(16)
+            ms16, kms16, _ = time_device(eng, torch, d, 16, args.steps, args.warmup, dist)
+            variants[f"{args.precision}_K16"] = {"evals_per_s": 16e3 / ms16, "ms_per_step": ms16, "kernel_ms": kms16,
+                                                  "shape": list(eng.shape())}
         if args.precision == "fp32":
             eng.close()
             eng = Engine.from_workload(wl, precision="fp64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
@@ -387,6 +396,19 @@ def run_gw(args, world, rank, local, dist):
                 eng.autotune(K)
                 msk, kmsk, _ = time_device(eng, torch, d, K, args.steps, args.warmup, dist)
                 variants[f"fp64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk}
+            if K < 256:
+                eng.close()
+                K2 = 256
+                eng = Engine.from_workload(wl, precision=args.precision, k_max=K2,
+                                           llh_type=llh_type_for(args.config), device=local)
+                eng.autotune(K2)
+                d2 = {"p": torch.from_numpy(wl.draw_points(K2, 4321 + rank)).cuda(),
+                      "s": torch.empty((K2, wl.n_bins), dtype=torch.float64, device="cuda")}
+                d2["s2"] = torch.empty_like(d2["s"])
+                d2["l"] = torch.empty(K2, dtype=torch.float64, device="cuda")
+                ms2, kms2, _ = time_device(eng, torch, d2, K2, max(3, args.steps // 4), args.warmup, dist)
+                variants[f"{args.precision}_K{K2}"] = {"evals_per_s": K2 * 1e3 / ms2, "ms_per_step": ms2,
+                                                        "kernel_ms": kms2, "shape": list(eng.shape())}
         eng.sync()
     eng.close()
 
@@ -413,10 +435,12 @@ def run_gw(args, world, rank, local, dist):
                        "parallelism": f"replicas x{world}", "tiles": layout["n_tiles"],
                        "payload_bytes": layout["payload_bytes"],
                        "kernel_shape": {"family": shape[0], "points_per_pass": shape[1], "threads": shape[2],
-                                        "stages": shape[3]}},
+                                        "stages": shape[3], "index": sidx,
+                                        "points_per_thread": sfull[2] if sfull else None,
+                                        "min_blocks_per_sm": sfull[5] if sfull else None}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": ("k_plain" if K == 1 else ("k_multi" if shape[0] == 1 else "k_batched")),
+                         "kernel": (plain_name if K == 1 else ("k_multi" if shape[0] == 1 else "k_batched")),
                          "kernel_ms": kernel_ms,
                          "algorithmic_bytes_per_launch": alg, "compute": compute},
             "cpu_baseline": cpu,

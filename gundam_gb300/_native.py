@@ -153,6 +153,10 @@ GW_SIGNATURES: dict[str, list] = {
     "gw_autotune": [_P, _I32],
     "gw_get_shape": [_P, _P, _P, _P, _P],
     "gw_set_shape": [_P, _I32, _I32, _I32, _I32],
+    "gw_set_shape_index": [_P, _I32],
+    "gw_get_shape_index": [_P, _P],
+    "gw_shape_count": [],
+    "gw_shape_at": [_I32, _P, _P, _P, _P, _P, _P],
     "gw_set_plain_kernel": [_P, _I32],
     "gw_get_plain_kernel": [_P, _P],
     "gw_set_event_weight_copy": [_P, _I32],

@@ -25,76 +25,6 @@ __device__ __forceinline__ T hermite(T p1, T m1, T p2, T m2, T fx) {
            m1) * fx + p1);
 }
 
-// Catmull-Rom spline on uniform knots, with (limit == true) the
-// Fritsch-Carlson slope limiter: CalculateMonotonicSpline.h:49-148 and
-// (limit == false) CalculateCompactSpline.h:48-126.
-// d = [low, step, y_0 .. y_{n-1}].
-template <typename T, bool limit>
-__device__ __forceinline__ T eval_catmull(const T* __restrict__ d, int n, T x, bool trunc) {
-  const T low = d[0];
-  const T step = d[1];
-  if (trunc) {  // MonotonicSpline.cpp:78-81
-    const T high = low + T(n - 1) * step;
-    if (x <= low) x = low;
-    else if (x >= high) x = high;
-  }
-  const T xx = (x - low) / step;
-  const int ix = (xx < T(0)) ? (int)(xx - T(1)) : (int)xx;
-  const int last = n - 2;
-  const int a = min(max(ix - 1, 0), last);
-  const int b = min(max(ix, 0), last);
-  const int c = min(max(ix + 1, 0), last);
-  const T* y = d + 2;
-  const T p2 = y[b];
-  const T p3 = y[b + 1];
-  const T fx = xx - T(b);
-  const T d21 = y[a + 1] - y[a];
-  const T d32 = p3 - p2;
-  const T d43 = y[c + 1] - y[c];
-  T m2 = T(0.5) * (d21 + d32);
-  T m3 = T(0.5) * (d32 + d43);
-  if (limit) {
-    if (d32 * d21 <= T(0)) m2 = T(0);
-    if (d43 * d32 <= T(0)) m3 = T(0);
-    const T ad21 = (d21 < T(0)) ? -d21 : d21;
-    const T ad32 = (d32 < T(0)) ? -d32 : d32;
-    const T ad43 = (d43 < T(0)) ? -d43 : d43;
-    const T delta2 = T(3) * ((ad21 < ad32) ? ad21 : ad32);
-    const T delta3 = T(3) * ((ad32 < ad43) ? ad32 : ad43);
-    if (m2 > delta2) m2 = delta2;
-    if (m2 < -delta2) m2 = -delta2;
-    if (m3 > delta3) m3 = delta3;
-    if (m3 < -delta3) m3 = -delta3;
-  }
-  const T v = ((((T(2) * p2 - T(2) * p3 + m3 + m2) * fx + T(3) * p3 - T(3) * p2 - m3 - T(2) * m2) * fx +
-                m2) * fx + p2);
-  return v;
-}
-
-// Hermite spline on uniform knots with stored slopes: CalculateUniformSpline.h:46-80.
-// d = [low, step, (y, dydx) x n].
-template <typename T>
-__device__ __forceinline__ T eval_uniform(const T* __restrict__ d, int n, T x, bool trunc) {
-  const T low = d[0];
-  const T step = d[1];
-  if (trunc) {  // UniformSpline.cpp:47-60
-    const T high = low + T(n - 1) * step;
-    if (x <= low) x = low;
-    else if (x >= high) x = high;
-  }
-  const T xx = (x - low) / step;
-  int ix = (int)xx;
-  if (ix < 0) ix = 0;
-  if (ix > n - 2) ix = n - 2;  // same interval choice as "2*ix+7>dim"
-  const T fx = xx - T(ix);
-  const T* k = d + 2 + 2 * ix;
-  const T p1 = k[0];
-  const T m1 = k[1] * step;
-  const T p2 = k[2];
-  const T m2 = k[3] * step;
-  return (hermite(p1, m1, p2, m2, fx));
-}
-
 // Hermite spline on non-uniform knots: CalculateGeneralSpline.h:51-197, with
 // its 5-step branch-free search (:135-159).  Here the payload drops the unused
 // [low, step] prefix: d = [(y, dydx, x) x n].
@@ -147,28 +77,49 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
   return (p1 + fx * m);
 }
 
-// Engine layout of the Catmull-Rom and uniform splines.  The host stores each
+// Catmull-Rom splines on uniform knots (CalculateMonotonicSpline.h:49-148 with
+// the Fritsch-Carlson limiter, CalculateCompactSpline.h:48-126 without) and
+// Hermite splines on uniform knots with stored slopes
+// (CalculateUniformSpline.h:46-80).  The host stores each
 // knot's value and its slope in index units (for Catmull-Rom splines the
 // slope after the Fritsch-Carlson limiter, for uniform splines dydx*step) and
 // 1/step instead of step: d = [low, 1/step, (y, s) x n].  Inside the knot
 // range this is exactly the Hermite cubic the reference evaluates; beyond the
 // ends the reference's clamped neighbour indices make the outer slope equal
 // the end difference (CalculateMonotonicSpline.h:66-103), restored here.
+//
+// The interval is i = clamp(floor(xx), 0, n - 2) and fx = xx - i; the
+// reference's index tests (ix < 0, ix > n - 2) are fx < 0 and fx >= 1.  In
+// FP32 the floor is one addition rounded toward minus infinity: for
+// |xx| < 2^22, xx + 1.5*2^23 lies where the float spacing is one, so the
+// rounded sum is 1.5*2^23 + floor(xx) exactly; larger |xx| still lands on the
+// correct side of the clamp.  The integer i is read from the mantissa of
+// i + 2^23.  No float<->int conversion instructions are issued.
 template <typename T, bool catmull>
 __device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, bool trunc) {
   T xx = (x - d[0]) * d[1];
-  if (trunc) xx = (xx < T(0)) ? T(0) : ((xx > T(n - 1)) ? T(n - 1) : xx);
-  const int ix = catmull ? ((xx < T(0)) ? (int)(xx - T(1)) : (int)xx) : (int)xx;
-  const int i = min(max(ix, 0), n - 2);
-  const T fx = xx - (T)i;
+  T fi;
+  int i;
+  if constexpr (sizeof(T) == 4) {
+    const float nm2 = __int_as_float(0x4B000000 | (n - 2)) - 8388608.0f;  // (float)(n - 2)
+    if (trunc) xx = fminf(fmaxf(xx, 0.0f), nm2 + 1.0f);
+    const float f = __fadd_rd(xx, 12582912.0f) - 12582912.0f;
+    fi = fminf(fmaxf(f, 0.0f), nm2);
+    i = __float_as_int(fi + 8388608.0f) - 0x4B000000;
+  } else {
+    if (trunc) xx = (xx < T(0)) ? T(0) : ((xx > T(n - 1)) ? T(n - 1) : xx);
+    i = min(max((int)xx, 0), n - 2);
+    fi = (T)i;
+  }
+  const T fx = xx - fi;
   const T* k = d + 2 + 2 * i;
   const T p1 = k[0];
   T m1 = k[1];
   const T p2 = k[2];
   T m2 = k[3];
   if (catmull) {
-    if (ix < 0) m2 = p2 - p1;
-    if (ix > n - 2) m1 = p2 - p1;
+    if (fx < T(0)) m2 = p2 - p1;
+    if (fx >= T(1)) m1 = p2 - p1;
   }
   return (hermite(p1, m1, p2, m2, fx));
 }

@@ -98,7 +98,7 @@ struct gw_engine {
   int kpad = 32;
   int n_slots = 0;
   int plain_grid = 1;
-  BatchedShape shape{0, 32, 2, 256, 1};
+  BatchedShape shape{0, 32, 2, 256, 1, 4};
   int batched_grid = 1;
   bool tuned = false;
   int max_fn_table = 0;
@@ -1094,8 +1094,8 @@ int build_and_upload(gw_engine* e) {
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
   e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bps * e->num_sms));
   const int K0 = e->cfg.k_max;
-  if (K0 >= 8) e->shape = BatchedShape{1, 8, 4, 256, 1};
-  else e->shape = BatchedShape{1, 4, 2, 256, 2};
+  if (K0 >= 8) e->shape = BatchedShape{1, 8, 4, 256, 1, 0};
+  else e->shape = BatchedShape{1, 4, 2, 256, 2, 0};
   const int bb = batched_blocks_per_sm(v, e->shape);
   if (bb < 1) return fail(e, GW_ERR_CUDA, "batched kernel does not fit on an SM");
   e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bb * e->num_sms));
@@ -1367,6 +1367,7 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
     } else if (b.kc > 2 * K) {
       continue;
     }
+    if (!batched_shape_covers(e->view, b, K)) continue;
     const int bps = batched_blocks_per_sm(e->view, b);
     if (bps < 1) continue;
     e->shape = b;
@@ -1402,19 +1403,57 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
 extern "C" int gw_set_shape(gw_engine* e, int32_t kind, int32_t kc, int32_t threads, int32_t stages) {
   if (!e) return GW_ERR_ARG;
   if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
-  GW_CUDA(e, cudaSetDevice(e->device));
   for (int i = 0; i < batched_shape_count(); ++i) {
     const BatchedShape b = batched_shape(i);
     const int per_pass = b.kind == 0 ? b.kc * b.kr : b.kc;
-    if (b.kind != kind || per_pass != kc || b.threads != threads || b.stages != stages) continue;
-    const int bps = batched_blocks_per_sm(e->view, b);
-    if (bps < 1) return fail(e, GW_ERR_ARG, "shape does not fit on an SM");
-    e->shape = b;
-    e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
-    e->clear_graphs();
-    return GW_OK;
+    if (b.kind == kind && per_pass == kc && b.threads == threads && b.stages == stages)
+      return gw_set_shape_index(e, i);
   }
   return fail(e, GW_ERR_ARG, "no compiled shape (%d, %d, %d, %d)", kind, kc, threads, stages);
+}
+
+extern "C" int gw_set_shape_index(gw_engine* e, int32_t i) {
+  if (!e) return GW_ERR_ARG;
+  if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
+  if (i < 0 || i >= batched_shape_count()) return fail(e, GW_ERR_ARG, "shape index %d out of range", i);
+  GW_CUDA(e, cudaSetDevice(e->device));
+  const BatchedShape b = batched_shape(i);
+  const int bps = batched_blocks_per_sm(e->view, b);
+  if (bps < 1) return fail(e, GW_ERR_ARG, "shape %d does not fit on an SM", i);
+  e->shape = b;
+  e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(e->view.n_tiles, (int64_t)bps * e->num_sms));
+  e->clear_graphs();
+  return GW_OK;
+}
+
+extern "C" int gw_get_shape_index(const gw_engine* e, int32_t* i) {
+  if (!e || !i) return GW_ERR_ARG;
+  *i = -1;
+  for (int j = 0; j < batched_shape_count(); ++j) {
+    const BatchedShape b = batched_shape(j);
+    if (b.kind == e->shape.kind && b.kc == e->shape.kc && b.kr == e->shape.kr && b.threads == e->shape.threads &&
+        b.stages == e->shape.stages && b.minb == e->shape.minb) {
+      *i = j;
+      break;
+    }
+  }
+  return GW_OK;
+}
+
+extern "C" int gw_shape_count(void) { return batched_shape_count(); }
+
+extern "C" int gw_shape_at(int32_t i, int32_t* kind, int32_t* kc, int32_t* kr, int32_t* threads, int32_t* stages,
+                           int32_t* min_blocks) {
+  if (i < 0 || i >= batched_shape_count() || !kind || !kc || !kr || !threads || !stages || !min_blocks)
+    return GW_ERR_ARG;
+  const BatchedShape b = batched_shape(i);
+  *kind = b.kind;
+  *kc = b.kind == 0 ? b.kc * b.kr : b.kc;
+  *kr = b.kr;
+  *threads = b.threads;
+  *stages = b.stages;
+  *min_blocks = b.minb;
+  return GW_OK;
 }
 
 extern "C" int gw_set_plain_kernel(gw_engine* e, int32_t kind) {

@@ -74,9 +74,10 @@ cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
 // Shape of a batched (K > 1) launch.  kind 0 = k_batched: lanes over points,
 // kc points per warp pass, kr points per lane.  kind 1 = k_multi: threads over
 // dials, kc points per chunk, kr points per thread.  threads per block and
-// payload stages for both.
+// payload stages for both; minb = CTAs per SM the kernel's register
+// allocation targets (its launch bounds; 0 = the compiler's choice).
 struct BatchedShape {
-  int kind, kc, kr, threads, stages;
+  int kind, kc, kr, threads, stages, minb;
 };
 int batched_shape_count();
 BatchedShape batched_shape(int i);
@@ -84,13 +85,16 @@ BatchedShape batched_shape(int i);
 // One compiled batched kernel: its function (for occupancy queries) and its
 // launcher, per precision [FP64, FP32].
 struct ShapeEntry {
-  int kind, kc, kr, threads, stages;
+  int kind, kc, kr, threads, stages, minb;
   const void* fn[2];
   void (*launch[2])(const DevView&, int, int, size_t, cudaStream_t);
 };
 int lane_shapes(const ShapeEntry** out);   // gw_lanes.cu
 int multi_shapes(const ShapeEntry** out);  // gw_multi.cu
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s);
+// True when every pass of the shape over K points stays inside the kpad
+// columns of the parameter and partial-sum arrays.
+bool batched_shape_covers(const DevView& v, const BatchedShape& b, int K);
 cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2, double* llh,
                             double* llh_stat, cudaStream_t s);
 

@@ -466,7 +466,7 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
   }
   const int nw = b.threads / 32;
   return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
-         (size_t)kMaxLocalBins * nw * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
+         (size_t)(nw + kMaxLocalBins - 1) * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
          (kMaxTileEvents + 1) * sizeof(uint16_t);
 }
 
@@ -493,13 +493,14 @@ int batched_shape_count() {
 
 BatchedShape batched_shape(int i) {
   const ShapeEntry& e = *shape_entry(i);
-  return BatchedShape{e.kind, e.kc, e.kr, e.threads, e.stages};
+  return BatchedShape{e.kind, e.kc, e.kr, e.threads, e.stages, e.minb};
 }
 
 static const ShapeEntry* find_shape(const BatchedShape& b) {
   for (int i = 0; i < batched_shape_count(); ++i) {
     const ShapeEntry* e = shape_entry(i);
-    if (e->kind == b.kind && e->kc == b.kc && e->kr == b.kr && e->threads == b.threads && e->stages == b.stages)
+    if (e->kind == b.kind && e->kc == b.kc && e->kr == b.kr && e->threads == b.threads && e->stages == b.stages &&
+        e->minb == b.minb)
       return e;
   }
   return nullptr;
@@ -579,9 +580,14 @@ cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+bool batched_shape_covers(const DevView& v, const BatchedShape& b, int K) {
+  const int per_pass = b.kind == 0 ? b.kc * b.kr : b.kc;
+  return K >= 1 && per_pass >= 1 && (int64_t)((K + per_pass - 1) / per_pass) * per_pass <= (int64_t)v.kpad;
+}
+
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s) {
   const ShapeEntry* e = find_shape(b);
-  if (!e) return cudaErrorInvalidValue;
+  if (!e || !batched_shape_covers(v, b, K)) return cudaErrorInvalidValue;
   e->launch[v.precision ? 1 : 0](v, K, grid, batched_smem_bytes(v, b), s);
   return cudaGetLastError();
 }

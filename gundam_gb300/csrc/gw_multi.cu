@@ -131,7 +131,7 @@ void launch_m(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
 }
 
 #define GW_MULTI(KCH, KR, ST)                                                                  \
-  {1, KCH, KR, 256, ST, {(const void*)k_multi<double, KCH, KR, ST>,                            \
+  {1, KCH, KR, 256, ST, 0, {(const void*)k_multi<double, KCH, KR, ST>,                         \
                          (const void*)k_multi<float, KCH, KR, ST>},                             \
    {launch_m<double, KCH, KR, ST>, launch_m<float, KCH, KR, ST>}}
 

@@ -161,6 +161,29 @@ class Engine:
     def set_shape(self, kind, points_per_pass, threads, stages):
         self._chk(self.lib.gw_set_shape(self._e, kind, points_per_pass, threads, stages))
 
+    def set_shape_index(self, i):
+        """Selects entry i of compiled_shapes()."""
+        self._chk(self.lib.gw_set_shape_index(self._e, int(i)))
+
+    def shape_index(self):
+        """Entry of compiled_shapes() in use by the batched path."""
+        i = C.c_int32()
+        self._chk(self.lib.gw_get_shape_index(self._e, C.byref(i)))
+        return i.value
+
+    @staticmethod
+    def compiled_shapes(lib=None):
+        """Every compiled batched shape: (family, points per pass, points per
+        thread, threads per block, payload stages, min CTAs per SM of its
+        launch bounds (0: the compiler's choice))."""
+        lib = lib or N.libgw()
+        out = []
+        v = [C.c_int32() for _ in range(6)]
+        for i in range(lib.gw_shape_count()):
+            N.check(lib.gw_shape_at(i, *[C.byref(x) for x in v]))
+            out.append(tuple(x.value for x in v))
+        return out
+
     def set_plain_kernel(self, kind): self._chk(self.lib.gw_set_plain_kernel(self._e, int(kind)))
 
     def plain_kernel(self) -> int:

@@ -1,14 +1,14 @@
 """A small, self-contained case for profiling one kernel under ncu.
 
-    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64} [n_events]
+    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64} [n_events] [shape_index]
     python -m gundam_gb300.profile_case train [steps]
     python -m gundam_gb300.profile_case substeps [n_sub]
 
 plain / batched: builds the C2-shaped workload with n_events events (default
 1,000,000: a payload above the 129 MB L2 but a few GB of device memory at
-most) and evaluates it four times: K = 1 (k_plain) or K = 64 with the batched
-shape the benchmark selects on this workload (k_batched, 64 points per pass,
-256 threads, one payload stage).
+most) and evaluates it four times: K = 1 (the K = 1 kernel) or K = 64 with
+batched shape `shape_index` (an entry of Engine.compiled_shapes(); without
+it the autotuner picks one first, and the chosen index is printed).
 
 train: the C2 surrogate network (200 -> 512 -> 512 -> 512 -> 3000, BF16)
 trained for `steps` (default 8) Adam steps of batch 2048 on a device-resident
@@ -69,11 +69,14 @@ def main(argv):
     K = 64 if mode == "batched" else 1
     eng = Engine.from_workload(wl, precision=precision, k_max=64)
     if mode == "batched":
-        eng.set_shape(0, 64, 256, 1)
+        if len(argv) > 3:
+            eng.set_shape_index(int(argv[3]))
+        else:
+            eng.autotune(64)
     pts = wl.draw_points(K, 5)
     for _ in range(4):
         eng.eval(pts)
-    print("ok", eng.layout()["payload_bytes"], eng.shape())
+    print("ok", eng.layout()["payload_bytes"], eng.shape(), "shape index", eng.shape_index())
 
 
 if __name__ == "__main__":

@@ -103,16 +103,18 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
         outs = (torch.empty((64, meta["bins"]), dtype=torch.float64, device="cuda"),
                 torch.empty((64, meta["bins"]), dtype=torch.float64, device="cuda"),
                 torch.empty(64, dtype=torch.float64, device="cuda"))
+        eng.autotune(1)
         ms1 = time_eval(eng, torch, 1, p_dev, outs)
         hw = max(hw, device_used_gb(torch) - base_used)
         r["plain_K1"] = {"ms_per_pass": ms1, "evals_per_s": 1e3 / ms1,
                          "hbm_gbs": bytes1 / (ms1 / 1e3) / 1e9, "frac": bytes1 / (ms1 / 1e3) / 1e9 / peak_bw,
-                         "algorithmic_bytes": bytes1}
+                         "algorithmic_bytes": bytes1, "kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()]}
         eng.autotune(64)
         ms64 = time_eval(eng, torch, 64, p_dev, outs)
         hw = max(hw, device_used_gb(torch) - base_used)
         r["batched_K64"] = {"ms_per_pass": ms64, "evals_per_s": 64e3 / ms64,
                             "hbm_gbs": bytes64 / (ms64 / 1e3) / 1e9, "shape": list(eng.shape()),
+                            "shape_entry": list(Engine.compiled_shapes()[eng.shape_index()]),
                             "algorithmic_bytes": bytes64}
         r["device_memory_high_water_gb"] = hw
         r.update(meta)

@@ -234,16 +234,31 @@ int gw_autotune(gw_engine* e, int32_t K);
  * GW_ERR_ARG when no such compiled shape exists or it does not fit. */
 int gw_set_shape(gw_engine* e, int32_t kind, int32_t points_per_pass, int32_t threads, int32_t stages);
 
-/* Copies the batched shape in use out: kernel family (0 = lanes over points,
- * 1 = threads over dials), parameter points per pass, threads per block,
- * payload stages. */
 /* The K = 1 kernel: 0 = one block pipeline per tile (k_plain), 1 =
  * warp-specialised (k_plain_ws: six warps evaluate the next tile's dials while
  * two form the current tile's products and bin partials).  gw_autotune(e, 1)
  * times both and keeps the faster.  Performance only: results are identical. */
 int gw_set_plain_kernel(gw_engine* e, int32_t kind);
 int gw_get_plain_kernel(const gw_engine* e, int32_t* kind);
+
+/* Copies the batched shape in use out: kernel family (0 = lanes over points,
+ * 1 = threads over dials), parameter points per pass, threads per block,
+ * payload stages. */
 int gw_get_shape(const gw_engine* e, int32_t* kind, int32_t* points_per_pass, int32_t* threads, int32_t* stages);
+
+/* The compiled batched shapes, for sweeps and tests.  gw_shape_count()
+ * entries; gw_shape_at copies entry i out: family, points per pass, points
+ * per thread, threads per block, payload stages and min_blocks (the CTAs per
+ * SM its launch bounds ask the compiler to fit; 0 = the compiler's choice).
+ * A shape may be compiled for several register targets; gw_set_shape takes
+ * the first.  Such variants give identical results.  gw_set_shape_index
+ * selects entry i (GW_ERR_ARG when out of range or it does not fit on an
+ * SM); gw_get_shape_index reports the entry in use. */
+int gw_shape_count(void);
+int gw_shape_at(int32_t i, int32_t* kind, int32_t* points_per_pass, int32_t* points_per_thread, int32_t* threads,
+                int32_t* stages, int32_t* min_blocks);
+int gw_set_shape_index(gw_engine* e, int32_t i);
+int gw_get_shape_index(const gw_engine* e, int32_t* i);
 
 /* Cache::Manager::SetIsEventWeightCopyEnabled (CacheManager.h:119). */
 int gw_set_event_weight_copy(gw_engine* e, int32_t enable);

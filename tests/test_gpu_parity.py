@@ -381,3 +381,37 @@ def test_eigen_decomposed_parameters(c1, c1_oracle):
     np.testing.assert_allclose(stat, r["llh_stat"], rtol=0, atol=1e-6)
     np.testing.assert_allclose(llh, r["llh"], rtol=1e-10, atol=1e-6)
     e2.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
+    """Every compiled batched kernel shape (both families, every register
+    target) on the workload with every dial type, K = 64 inflated prior draws
+    (extrapolation beyond the knot ranges included), against the oracle; the
+    register targets of one shape give identical results."""
+    K = 64
+    eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    pts = mixed.draw_points(K, 77, inflate=2.5)
+    ref = mixed_oracle.eval(pts)
+    tol = (FP64_BIN_REL, FP64_LLH_ABS) if prec == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
+    first = {}
+    tried = 0
+    for i, (kind, ppp, ppt, threads, stages, minb) in enumerate(Engine.compiled_shapes()):
+        if ppp > K:
+            continue  # a 128-point pass would run past the engine's 64 padded point columns
+        try:
+            eng.set_shape_index(i)
+        except RuntimeError:
+            continue  # does not fit on an SM at this tile size
+        assert eng.shape_index() == i and eng.shape() == (kind, ppp, threads, stages)
+        out = [np.array(x, copy=True) for x in eng.eval(pts)]
+        _check(out, ref, *tol, f"shape {(kind, ppp, ppt, threads, stages, minb)}")
+        key = (kind, ppp, ppt, threads, stages)
+        if key in first:
+            for x, y in zip(first[key], out):
+                np.testing.assert_array_equal(x, y)
+        else:
+            first[key] = out
+        tried += 1
+    assert tried >= 10
+    eng.close()
