@@ -371,12 +371,24 @@ def run_gw(args, world, rank, local, dist):
     plain_name = ["k_plain", "k_plain_ws"][eng.plain_kernel()]
     variants = {}
     if not args.no_variants:
-        # the same engine at K=1 (plain kernel), and the FP64 engine at K=1
+        # K = 1 (the plain kernel) on this engine, whose splines carry precomputed
+        # slopes for the batched kernel, and on a K = 1 engine (knot values)
         eng.autotune(1)
         ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-        variants[f"{args.precision}_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
+        variants[f"{args.precision}_K1_slopes_layout"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
-            "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9}
+            "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9,
+            "payload_bytes": layout["payload_bytes"]}
+        e1 = Engine.from_workload(wl, precision=args.precision, k_max=1, llh_type=llh_type_for(args.config),
+                                  device=local)
+        e1.autotune(1)
+        ms1, kms1, _ = time_device(e1, torch, d, 1, args.steps, args.warmup, dist)
+        variants[f"{args.precision}_K1"] = {"kernel": ["k_plain", "k_plain_ws"][e1.plain_kernel()],
+            "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
+            "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9,
+            "kernel_frac_of_hbm_peak": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9 / peak,
+            "payload_bytes": e1.layout()["payload_bytes"], "spline_layout": "knots"}
+        e1.close()
         if K > 16:
             # C3 at the C2 size: K = 16 on this engine, K = 256 on one sized for it
             eng.autotune(16)

@@ -34,6 +34,8 @@ GW_DIAL_KRIGED = 10
 
 GW_FP64 = 0
 GW_FP32 = 1
+GW_FLAG_SPLINE_KNOTS = 1
+GW_FLAG_SPLINE_SLOPES = 2
 
 GW_LLH_NONE = 0
 GW_LLH_POISSON = 1

@@ -82,6 +82,20 @@ __device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned 
   if (bytes > 0) bulk_load(buf, v.payload + td.payload_off, bytes, bar);
 }
 
+// Thread 0: the same, plus the tile's headers into hbuf under the same
+// barrier.  A tile's headers start at an even index (16-byte aligned) and the
+// array is padded, so the copy is whole 16-byte units: ceil(ndials / 2) * 16
+// bytes <= tile_hdr_bytes.
+__device__ __forceinline__ void issue_tile_hdr(const DevView& v, int tile, unsigned char* buf, uint64_t* hbuf,
+                                               uint64_t* bar) {
+  const TileDesc td = v.tiles[tile];
+  const uint32_t bytes = (uint32_t)td.payload_16b * 16u;
+  const uint32_t hbytes = (((uint32_t)td.ndials + 1u) / 2u) * 16u;
+  mbar_expect_tx(bar, bytes + hbytes);
+  if (bytes > 0) bulk_load(buf, v.payload + td.payload_off, bytes, bar);
+  if (hbytes > 0) bulk_load(hbuf, v.hdr + td.dial0, hbytes, bar);
+}
+
 // ---------------------------------------------------------------------------
 // One dial at KR parameter points (k0, k0 + kstep, ...): the header is
 // decoded, the type dispatched and the response clamp loaded once; the KR
@@ -135,9 +149,12 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       if (lo < T(-1e20)) lo = T(-1e20);
       if (hi > T(1e20)) hi = T(1e20);
       if (type == kMonotonic) {
+        if (v.spline_knots) {
 #pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
+          for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, true>(d, n, x[j], trunc);
+        } else {
+#pragma unroll
+          for (int j = 0; j < KR; ++j) val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
         }
       } else if (type == kUniform) {
 #pragma unroll
@@ -155,9 +172,12 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
       } else if (type == kCompact) {
+        if (v.spline_knots) {
 #pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
+          for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, false>(d, n, x[j], trunc);
+        } else {
+#pragma unroll
+          for (int j = 0; j < KR; ++j) val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
         }
       } else if (type == kBicubic) {
         const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;

@@ -95,11 +95,8 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
 // rounded sum is 1.5*2^23 + floor(xx) exactly; larger |xx| still lands on the
 // correct side of the clamp.  The integer i is read from the mantissa of
 // i + 2^23.  No float<->int conversion instructions are issued.
-template <typename T, bool catmull>
-__device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, bool trunc) {
-  T xx = (x - d[0]) * d[1];
-  T fi;
-  int i;
+template <typename T>
+__device__ __forceinline__ void knot_interval(T& xx, int n, bool trunc, T& fi, int& i) {
   if constexpr (sizeof(T) == 4) {
     const float nm2 = __int_as_float(0x4B000000 | (n - 2)) - 8388608.0f;  // (float)(n - 2)
     if (trunc) xx = fminf(fmaxf(xx, 0.0f), nm2 + 1.0f);
@@ -111,6 +108,14 @@ __device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, 
     i = min(max((int)xx, 0), n - 2);
     fi = (T)i;
   }
+}
+
+template <typename T, bool catmull>
+__device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, bool trunc) {
+  T xx = (x - d[0]) * d[1];
+  T fi;
+  int i;
+  knot_interval(xx, n, trunc, fi, i);
   const T fx = xx - fi;
   const T* k = d + 2 + 2 * i;
   const T p1 = k[0];
@@ -121,6 +126,52 @@ __device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, 
     if (fx < T(0)) m2 = p2 - p1;
     if (fx >= T(1)) m1 = p2 - p1;
   }
+  return (hermite(p1, m1, p2, m2, fx));
+}
+
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// Catmull-Rom knot slope from the differences on either side, with the
+// Fritsch-Carlson limiter when `limit` (CalculateMonotonicSpline.h:66-127);
+// the same operations as the host's precomputed slopes.  The halving is an
+// explicitly rounded multiply, so the compiler cannot fuse it into the
+// Hermite sums that follow: the slope is rounded exactly as the host's.
+template <typename T, bool limit>
+__device__ __forceinline__ T knot_slope(T dl, T dr) {
+  T s = mul_rn(T(0.5), dl + dr);
+  if (limit) {
+    if (dr * dl <= T(0)) s = T(0);
+    const T adl = (dl < T(0)) ? -dl : dl;
+    const T adr = (dr < T(0)) ? -dr : dr;
+    const T delta = T(3) * ((adl < adr) ? adl : adr);
+    if (s > delta) s = delta;
+    if (s < -delta) s = -delta;
+  }
+  return s;
+}
+
+// The same Catmull-Rom splines stored as knot values only, the reference's
+// data d = [low, 1/step, y_0 .. y_{n-1}]: the two slopes of the interval are
+// formed here from its neighbours (an end knot's slope is the end
+// difference, which knot_slope returns for equal sides).
+template <typename T, bool limit>
+__device__ __forceinline__ T eval_knots(const T* __restrict__ d, int n, T x, bool trunc) {
+  T xx = (x - d[0]) * d[1];
+  T fi;
+  int i;
+  knot_interval(xx, n, trunc, fi, i);
+  const T fx = xx - fi;
+  const T* y = d + 2;
+  const T p1 = y[i];
+  const T p2 = y[i + 1];
+  const T dc = p2 - p1;
+  const T dl = (i > 0) ? p1 - y[i - 1] : dc;
+  const T dr = (i + 2 < n) ? y[i + 2] - p2 : dc;
+  T m1 = knot_slope<T, limit>(dl, dc);
+  T m2 = knot_slope<T, limit>(dc, dr);
+  if (fx < T(0)) m2 = dc;
+  if (fx >= T(1)) m1 = dc;
   return (hermite(p1, m1, p2, m2, fx));
 }
 

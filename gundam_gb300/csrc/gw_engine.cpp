@@ -187,10 +187,11 @@ extern "C" int gw_create(const gw_config* c, gw_engine** out) {
   if (!c || !out) return fail(nullptr, GW_ERR_ARG, "null argument");
   *out = nullptr;
   if (c->n_results < 0 || c->n_params < 1 || c->n_params > 8192 || c->n_bins < 1 || c->k_max < 1 ||
-      c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32) || c->flags != 0)
+      c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32) ||
+      (c->flags != 0 && c->flags != GW_FLAG_SPLINE_KNOTS && c->flags != GW_FLAG_SPLINE_SLOPES))
     return fail(nullptr, GW_ERR_ARG,
-                "bad gw_config (n_results=%d n_params=%d n_bins=%d k_max=%d precision=%d)",
-                c->n_results, c->n_params, c->n_bins, c->k_max, c->precision);
+                "bad gw_config (n_results=%d n_params=%d n_bins=%d k_max=%d precision=%d flags=%d)",
+                c->n_results, c->n_params, c->n_bins, c->k_max, c->precision, c->flags);
   std::unique_ptr<gw_engine> e(new (std::nothrow) gw_engine());
   if (!e) return fail(nullptr, GW_ERR_NOMEM, "host allocation failed");
   e->cfg = *c;
@@ -626,10 +627,14 @@ void write_payload(const DialRec& r, const double* d, T* out) {
 // forms from its neighbours (with the Fritsch-Carlson limiter for monotonic
 // splines); the end knots get the end difference.  Computed here in FP64.
 template <typename T>
-void write_prepared(const DialRec& r, const double* d, int n, T* out) {
+void write_prepared(const DialRec& r, const double* d, int n, T* out, bool knots) {
   const double low = d[0], step = d[1];
   out[0] = (T)low;
   out[1] = (T)(1.0 / step);
+  if (knots && r.type != kUniform) {  // [low, 1/step, y x n]: slopes formed in the kernel
+    for (int k = 0; k < n; ++k) out[2 + k] = (T)d[2 + k];
+    return;
+  }
   if (r.type == kUniform) {
     for (int k = 0; k < n; ++k) {
       out[2 + 2 * k] = (T)d[2 + 2 * k];
@@ -663,9 +668,8 @@ void write_prepared(const DialRec& r, const double* d, int n, T* out) {
 // Stored elements of a dial in the engine precision.  Non-empty payloads are
 // padded to an odd element count: threads that read consecutive same-type
 // dials then hit distinct shared-memory banks.
-int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool fp32) {
-  (void)fp32;
-  int32_t el = (r.type == kMonotonic || r.type == kCompact) ? 2 + 2 * n : raw;
+int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool knots) {
+  int32_t el = (r.type == kMonotonic || r.type == kCompact) ? (knots ? 2 + n : 2 + 2 * n) : raw;
   if (el > 0 && (el & 1) == 0) ++el;
   return el;
 }
@@ -686,6 +690,10 @@ int build_and_upload(gw_engine* e) {
   const int B = e->cfg.n_bins;
   const int64_t D = (int64_t)e->dials.size();
   const size_t tsz = sizeof(T);
+  // stored form of Catmull-Rom splines (gw_config.flags; by default knot
+  // values for FP32 K = 1 engines, precomputed slopes otherwise)
+  const bool knots = e->cfg.flags == GW_FLAG_SPLINE_KNOTS ||
+                     (e->cfg.flags == 0 && e->cfg.k_max == 1 && tsz == 4);
 
   // 1. every result needs a bin (CacheManager.cpp:727-729 "Histogram cells are missing")
   for (int r = 0; r < N; ++r)
@@ -724,7 +732,7 @@ int build_and_upload(gw_engine* e) {
             int64_t exp = -1;
             bad.compare_exchange_strong(exp, i);
           }
-          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, tsz == 4);
+          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, knots);
           pn[(size_t)i] = n;
         }
       });
@@ -748,7 +756,11 @@ int build_and_upload(gw_engine* e) {
   }
 
   // 4. tiles
-  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : 24576) / (int64_t)tsz;
+  // default tile payload: 28 KB in FP32, 32 KB in FP64 (fastest of a 12-32 KB
+  // sweep on the 5M-event mixed workload at K = 1 and K = 64; larger FP32 tiles
+  // cost the K = 1 kernel its third CTA per SM)
+  const int64_t tile_default = tsz == 4 ? 28672 : 32768;
+  int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : tile_default) / (int64_t)tsz;
   cap_elems = std::min<int64_t>(cap_elems, kMaxPayloadElems);
   cap_elems = std::max<int64_t>(cap_elems, 64);
   std::vector<TilePlan> tiles;
@@ -783,16 +795,23 @@ int build_and_upload(gw_engine* e) {
   }
   const int64_t T_ = (int64_t)tiles.size();
   if (T_ > INT32_MAX) return fail(e, GW_ERR_LIMIT, "too many tiles");
+  // every tile's headers start on a 16-byte boundary (an even header index),
+  // so one bulk copy moves them with the payload
+  int64_t hdr_total = 0;
+  int32_t max_tile_dials = 0;
   {
     int64_t d0 = 0;
     uint64_t off = 0;
     for (TilePlan& t : tiles) {
       t.dial0 = d0;
       d0 += t.ndials;
+      d0 = (d0 + 1) & ~(int64_t)1;
+      max_tile_dials = std::max(max_tile_dials, t.ndials);
       t.payload_off = off;
       const uint64_t bytes = ((uint64_t)t.payload_elems * tsz + 15) & ~(uint64_t)15;
       off += bytes;
     }
+    hdr_total = d0;
   }
   const uint64_t payload_total = T_ ? tiles.back().payload_off +
                                           (((uint64_t)tiles.back().payload_elems * tsz + 15) & ~(uint64_t)15)
@@ -824,7 +843,7 @@ int build_and_upload(gw_engine* e) {
 
   // 6. pack tiles (parallel over tiles)
   std::vector<TileDesc> tdesc((size_t)T_);
-  std::vector<uint64_t> hdr((size_t)D);
+  std::vector<uint64_t> hdr((size_t)hdr_total, 0);
   std::vector<unsigned char> payload((size_t)payload_total, 0);
   std::vector<uint16_t> evinfo((size_t)N);
   std::vector<T> w0((size_t)N);
@@ -860,7 +879,7 @@ int build_and_upload(gw_engine* e) {
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
             hdr[(size_t)(tp.dial0 + j)] = make_header(r.type, pn[(size_t)di], slot, off, p0, p1);
             if (r.type == kMonotonic || r.type == kCompact || r.type == kUniform)
-              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off);
+              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off, knots);
             else
               write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
             off += pel[(size_t)di];
@@ -930,6 +949,8 @@ int build_and_upload(gw_engine* e) {
   v.has_cap = e->has_cap ? 1 : 0;
   v.cap = e->cap;
   v.tile_payload_bytes = (int)(((cap_elems * tsz) + 127) & ~(int64_t)127);
+  v.tile_hdr_bytes = std::max(16, ((max_tile_dials + 1) / 2) * 16);
+  v.spline_knots = knots ? 1 : 0;
 
   // slack after the per-dial and per-event arrays (reads rounded out to
   // 16-byte boundaries stay inside the allocation)
@@ -1172,6 +1193,10 @@ static int launch_chain(gw_engine* e, const double* d_params, int K, double* d_s
   if (K == 1) {
     GW_CUDA(e, launch_plain(v, e->plain_grid, s));
   } else {
+    if (!batched_shape_covers(v, e->shape, K))
+      return fail(e, GW_ERR_ARG, "the selected batched shape (%d points per pass) does not cover K = %d within "
+                  "the engine's %d padded point columns; select another shape or autotune for this K",
+                  e->shape.kind == 0 ? e->shape.kc * e->shape.kr : e->shape.kc, K, v.kpad);
     GW_CUDA(e, launch_batched(v, K, e->shape, e->batched_grid, s));
   }
   if (ev_end) GW_CUDA(e, cudaEventRecord(ev_end, s));

@@ -28,6 +28,8 @@ struct DevView {
   int n_tables;
   int n_table_fns;
   int tile_payload_bytes;  // shared-memory bytes reserved per payload stage
+  int tile_hdr_bytes;      // shared-memory bytes for one tile's headers (16-byte multiple)
+  int spline_knots;        // 1: Catmull-Rom payloads hold knot values only (slopes formed on the device)
   double cap;
 
   const TileDesc* tiles;

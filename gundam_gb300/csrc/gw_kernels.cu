@@ -252,8 +252,10 @@ template <typename T>
 __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain_ws(const DevView v) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
-  T* dval = (T*)(smem + 2 * TB);                          // [2][1024]
-  double* wsh = (double*)(smem + 2 * TB + 2048 * sizeof(T));  // [kMaxTileEvents]
+  const int HB = v.tile_hdr_bytes;
+  uint64_t* shdr = (uint64_t*)(smem + 2 * TB);                // [2][HB / 8], tile order
+  T* dval = (T*)(smem + 2 * TB + 2 * HB);                     // [2][1024]
+  double* wsh = (double*)(smem + 2 * TB + 2 * HB + 2048 * sizeof(T));  // [kMaxTileEvents]
   uint16_t* sev = (uint16_t*)(wsh + kMaxTileEvents);      // [kMaxTileEvents]
   __shared__ uint64_t bar[2];
   __shared__ int s_bstart[kMaxLocalBins], s_bend[kMaxLocalBins];
@@ -262,36 +264,23 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
   const int tid = threadIdx.x;
   const int ntile = (int)blockIdx.x < v.n_tiles ? (v.n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
                                                 : 0;
+  const int hstride = HB / (int)sizeof(uint64_t);
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
     s_fail = 0;
-    if (ntile > 0) issue_tile(v, blockIdx.x, smem, &bar[0]);
-    if (ntile > 1) issue_tile(v, blockIdx.x + gridDim.x, smem + TB, &bar[1]);
+    if (ntile > 0) issue_tile_hdr(v, blockIdx.x, smem, shdr, &bar[0]);
+    if (ntile > 1) issue_tile_hdr(v, blockIdx.x + gridDim.x, smem + TB, shdr + hstride, &bar[1]);
   }
   __syncthreads();
 
   if (tid < kWsEval) {
-    // software pipeline of the per-tile loads: the headers of tile it + 1 are
-    // loaded at the end of iteration it from the descriptor fields loaded
-    // during iteration it - 1, so no global load sits on a tile's critical
-    // path (the evaluators need only the first dial and the dial count)
-    int nd = 0, d0 = 0, nd_next = 0, d0_next = 0;
-    if (ntile > 0) {
-      nd = v.tiles[blockIdx.x].ndials;
-      d0 = (int)v.tiles[blockIdx.x].dial0;
-    }
-    uint64_t h[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      const int i = tid + j * kWsEval;
-      h[j] = (i < nd) ? v.hdr[d0 + i] : 0ull;
-    }
-    if (ntile > 1) {
-      nd_next = v.tiles[blockIdx.x + gridDim.x].ndials;
-      d0_next = (int)v.tiles[blockIdx.x + gridDim.x].dial0;
-    }
+    // a tile's payload and headers arrive together by bulk copy; only the
+    // dial count comes from the descriptor, loaded one tile ahead
+    int nd = 0, nd_next = 0;
+    if (ntile > 0) nd = v.tiles[blockIdx.x].ndials;
+    if (ntile > 1) nd_next = v.tiles[blockIdx.x + gridDim.x].ndials;
     for (int it = 0; it < ntile; ++it) {
       const int tile = blockIdx.x + it * gridDim.x;
       const int st = it & 1;
@@ -301,32 +290,22 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
       T* dv = dval + st * 1024;
       if (ok) {
         const T* pl = (const T*)(smem + st * TB);
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-          const int i = tid + j * kWsEval;
-          if (i < nd) {
-            T val[1];
-            dial_values<T, 1>(v, h[j], pl, 0, 0, val);
-            dv[hdr_slot(h[j])] = val[0];
-          }
+        const uint64_t* hs = shdr + st * hstride;
+        for (int i = tid; i < nd; i += kWsEval) {
+          const uint64_t h = hs[i];
+          T val[1];
+          dial_values<T, 1>(v, h, pl, 0, 0, val);
+          dv[hdr_slot(h)] = val[0];
         }
       }
       named_arrive(kBarFull + st, kPlainThreads);
       if (it + 1 < ntile) {
         nd = nd_next;
-        d0 = d0_next;
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-          const int i = tid + j * kWsEval;
-          h[j] = (i < nd) ? v.hdr[d0 + i] : 0ull;
-        }
-        if (it + 2 < ntile) {
-          nd_next = v.tiles[tile + 2 * gridDim.x].ndials;
-          d0_next = (int)v.tiles[tile + 2 * gridDim.x].dial0;
-        }
+        if (it + 2 < ntile) nd_next = v.tiles[tile + 2 * gridDim.x].ndials;
       }
-      named_sync(kBarEval, kWsEval);  // stage st fully read
-      if (tid == 0 && it + 2 < ntile) issue_tile(v, tile + 2 * gridDim.x, smem + st * TB, &bar[st]);
+      named_sync(kBarEval, kWsEval);  // stage st (payload and headers) fully read
+      if (tid == 0 && it + 2 < ntile)
+        issue_tile_hdr(v, tile + 2 * gridDim.x, smem + st * TB, shdr + st * hstride, &bar[st]);
     }
   } else {
     const int r = tid - kWsEval;
@@ -453,7 +432,8 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
 size_t plain_smem_bytes(const DevView& v) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
   const size_t dv = (v.plain_kind == 1 ? 2048 : 1024) * tsz;
-  return 2 * (size_t)v.tile_payload_bytes + dv + kMaxTileEvents * sizeof(double) +
+  const size_t hb = v.plain_kind == 1 ? 2 * (size_t)v.tile_hdr_bytes : 0;
+  return 2 * (size_t)v.tile_payload_bytes + hb + dv + kMaxTileEvents * sizeof(double) +
          kMaxTileEvents * sizeof(uint16_t);
 }
 

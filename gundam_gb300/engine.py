@@ -24,10 +24,14 @@ def _c(a, dtype):
 
 class Engine:
     def __init__(self, n_results: int, n_params: int, n_bins: int, k_max: int = 1, precision: str = "fp64",
-                 device: int = 0, tile_bytes: int = 0):
+                 device: int = 0, tile_bytes: int = 0, spline_layout: str = "auto"):
+        """spline_layout: stored form of Catmull-Rom splines, "knots" (knot
+        values, slopes formed on the device), "slopes" (slopes precomputed on
+        the host) or "auto" (knots for an FP32 engine with k_max == 1)."""
         self.lib = N.libgw()
+        flags = {"auto": 0, "knots": N.GW_FLAG_SPLINE_KNOTS, "slopes": N.GW_FLAG_SPLINE_SLOPES}[spline_layout]
         cfg = N.GwConfig(int(n_results), int(n_params), int(n_bins), int(k_max),
-                         N.GW_FP32 if precision == "fp32" else N.GW_FP64, int(device), int(tile_bytes), 0)
+                         N.GW_FP32 if precision == "fp32" else N.GW_FP64, int(device), int(tile_bytes), flags)
         p = C.c_void_p()
         N.check(self.lib.gw_create(C.byref(cfg), C.byref(p)), None)
         self._e = p
@@ -234,7 +238,7 @@ class Engine:
     # ---- convenience: load a generated workload ----
     @classmethod
     def from_workload(cls, wl, precision="fp64", k_max=1, llh_type=None, prior=True, device=0, tile_bytes=0,
-                      per_dial=False, initialize=True) -> "Engine":
+                      per_dial=False, initialize=True, spline_layout="auto") -> "Engine":
         """Builds an engine holding `wl` the way Cache::Manager::Update fills its caches.
 
         per_dial=True issues one call per dial (the reference's AddSpline /
@@ -242,7 +246,7 @@ class Engine:
         initialize=False stops before gw_initialize (the engine holds its own
         copies by then, so a large workload can be released first)."""
         e = cls(wl.n_events, wl.n_params, wl.n_bins, k_max=k_max, precision=precision, device=device,
-                tile_bytes=tile_bytes)
+                tile_bytes=tile_bytes, spline_layout=spline_layout)
         for p in range(wl.n_params):
             if wl.mirror_lo[p] > -np.finfo(np.float64).max:
                 e.set_lower_mirror(p, float(wl.mirror_lo[p]))

@@ -6,7 +6,8 @@
 
 plain / batched: builds the C2-shaped workload with n_events events (default
 1,000,000: a payload above the 129 MB L2 but a few GB of device memory at
-most) and evaluates it four times: K = 1 (the K = 1 kernel) or K = 64 with
+most) and evaluates it four times: K = 1 (the K = 1 kernel, on a K = 1
+engine: Catmull-Rom splines stored as knot values in FP32) or K = 64 with
 batched shape `shape_index` (an entry of Engine.compiled_shapes(); without
 it the autotuner picks one first, and the chosen index is printed).
 
@@ -67,7 +68,7 @@ def main(argv):
     n = int(argv[2]) if len(argv) > 2 else 1000000
     wl = Workload("c2", n_events=n, seed=2)
     K = 64 if mode == "batched" else 1
-    eng = Engine.from_workload(wl, precision=precision, k_max=64)
+    eng = Engine.from_workload(wl, precision=precision, k_max=K)
     if mode == "batched":
         if len(argv) > 3:
             eng.set_shape_index(int(argv[3]))

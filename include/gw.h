@@ -67,6 +67,21 @@ enum {
   GW_FP32 = 1  /* dials + weight product in FP32; bin sums, sum of w^2, LLH in FP64 */
 };
 
+/* ---- gw_config.flags: stored form of Catmull-Rom (monotonic, compact)
+ * splines.  Knot values only, [low, 1/step, y x n], the reference's own data,
+ * with the knot slopes formed in the kernel (fewer bytes per evaluation); or
+ * with the slopes precomputed on the host, [low, 1/step, (y, slope) x n]
+ * (less arithmetic per evaluation).  Neither flag: knot values for FP32
+ * engines with k_max == 1 (a bandwidth-bound evaluation), precomputed slopes
+ * otherwise (batched evaluation, and FP64, which GB300's FP64 rate makes
+ * arithmetic-bound).  Results agree within the precision's rounding; in FP64
+ * the per-event weights are identical (the bin sums then differ only in the
+ * grouping of their FP64 partial sums, as the tiles are cut differently). */
+enum {
+  GW_FLAG_SPLINE_KNOTS = 1,
+  GW_FLAG_SPLINE_SLOPES = 2
+};
+
 /* ---- likelihood evaluated after the histogram step --------------------- */
 enum {
   GW_LLH_NONE = 0,
@@ -93,8 +108,8 @@ typedef struct gw_config {
   int32_t k_max;      /* largest number of parameter points per gw_eval (>= 1) */
   int32_t precision;  /* GW_FP64 or GW_FP32 */
   int32_t device;     /* CUDA device ordinal */
-  int32_t tile_bytes; /* payload bytes per tile; 0 = default */
-  int32_t flags;      /* reserved, must be 0 */
+  int32_t tile_bytes; /* payload bytes per tile; 0 = default (28672 FP32, 32768 FP64) */
+  int32_t flags;      /* 0 or one GW_FLAG_SPLINE_* value */
 } gw_config;
 
 /* ---- engine lifetime --------------------------------------------------- */

@@ -124,6 +124,12 @@ def test_bad_config_rejected():
     p = C.c_void_p()
     assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
     assert "bad gw_config" in N.last_error(None)
+    cfg = N.GwConfig(10, 2, 1, 1, 0, 0, 0, N.GW_FLAG_SPLINE_KNOTS | N.GW_FLAG_SPLINE_SLOPES)
+    assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
+    for flags in (0, N.GW_FLAG_SPLINE_KNOTS, N.GW_FLAG_SPLINE_SLOPES):
+        cfg = N.GwConfig(10, 2, 1, 1, 0, 0, 0, flags)
+        assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_OK
+        lib.gw_destroy(p)
 
 
 def test_eigen_block_validation():
@@ -146,3 +152,24 @@ def test_eigen_block_validation():
     assert lib.gw_add_eigen_block(e, 3, 3, bad.ctypes.data_as(C.c_void_p)) == N.GW_ERR_NOT_FINITE
     assert lib.gw_add_eigen_block(e, 3, 3, p) == N.GW_OK
     lib.gw_destroy(e)
+
+
+def test_compiled_shape_list():
+    """gw_shape_count / gw_shape_at list every compiled batched kernel shape
+    (no device needed); out-of-range entries and selection before
+    gw_initialize are argument / state errors."""
+    shapes = Engine.compiled_shapes()
+    assert len(shapes) >= 10
+    for kind, ppp, ppt, threads, stages, minb in shapes:
+        assert kind in (0, 1) and threads in (128, 256) and stages in (1, 2) and minb >= 0
+        if kind == 0:
+            assert ppp % ppt == 0 and ppp // ppt in (8, 16, 32)
+    assert len(set(shapes)) == len(shapes)
+    v = [C.c_int32() for _ in range(6)]
+    lib = N.libgw()
+    assert lib.gw_shape_at(len(shapes), *[C.byref(x) for x in v]) == N.GW_ERR_ARG
+    assert lib.gw_shape_at(-1, *[C.byref(x) for x in v]) == N.GW_ERR_ARG
+    e = _engine()
+    with pytest.raises(N.GwError):
+        e.set_shape_index(0)
+    e.close()

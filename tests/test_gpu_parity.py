@@ -415,3 +415,54 @@ def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
         tried += 1
     assert tried >= 10
     eng.close()
+
+
+def test_shape_that_overruns_the_padded_points_is_refused(c1, c1_oracle):
+    """K = 150 pads to 192 point columns: a 128-point pass would need 256, so
+    the launch is refused with an error (never a read past the arrays); the
+    autotuner only picks shapes that fit, and those agree with the oracle."""
+    K = 150
+    eng = Engine.from_workload(c1, precision="fp32", k_max=K, llh_type=N.GW_LLH_POISSON)
+    pts = c1.draw_points(K, 21)
+    eng.set_shape(0, 128, 128, 1)
+    with pytest.raises(N.GwError, match="does not cover"):
+        eng.eval(pts)
+    eng.autotune(K)
+    kind, ppp, _, _ = eng.shape()
+    assert ppp <= 64 or kind == 1
+    _check(eng.eval(pts), c1_oracle.eval(pts), FP32_BIN_REL, FP32_LLH_ABS)
+    eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_spline_layouts_agree(mixed, mixed_oracle, prec):
+    """Catmull-Rom splines stored as knot values (the slopes formed on the
+    device) or with slopes precomputed on the host: both within tolerance of
+    the oracle through the K = 1 and the batched kernels.  In FP64 the
+    per-event weights are identical; the bin sums differ only in rounding,
+    because the smaller payload cuts different tiles and so groups the FP64
+    partial sums differently.  The knot form packs fewer bytes, and an FP32
+    K = 1 engine picks it."""
+    llh = N.GW_LLH_BARLOW_BEESTON_OA2021
+    pts = mixed.draw_points(4, 61, inflate=2.0)
+    ref = mixed_oracle.eval(pts)
+    tol = (FP64_BIN_REL, FP64_LLH_ABS) if prec == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
+    out = {}
+    for layout in ("knots", "slopes"):
+        eng = Engine.from_workload(mixed, precision=prec, k_max=4, llh_type=llh, spline_layout=layout)
+        eng.set_event_weight_copy(True)
+        weights = []
+        for i in range(len(pts)):
+            r = eng.eval(pts[i:i + 1])
+            _check(r, {k: ref[k][i:i + 1] for k in ref}, *tol, f"{layout} K=1 point {i}")
+            weights.append(eng.event_weights().copy())
+        _check(eng.eval(pts), ref, *tol, f"{layout} K=4")
+        out[layout] = (weights, eng.layout()["payload_bytes"])
+        eng.close()
+    if prec == "fp64":
+        for wk, ws in zip(out["knots"][0], out["slopes"][0]):
+            np.testing.assert_array_equal(wk, ws)
+    assert out["knots"][1] < out["slopes"][1]
+    auto = Engine.from_workload(mixed, precision=prec, k_max=1, llh_type=llh)
+    assert auto.layout()["payload_bytes"] == out["knots" if prec == "fp32" else "slopes"][1]
+    auto.close()
