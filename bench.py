@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true")
-    ap.add_argument("--mcmc-steps", type=int, default=3000)
+    ap.add_argument("--mcmc-steps", type=int, default=6000)
     ap.add_argument("--mcmc-train", type=int, default=65536)
     ap.add_argument("--mcmc-epochs", type=int, default=50)
     ap.add_argument("--mcmc-nsub", type=int, default=40)
