@@ -46,8 +46,8 @@ def parse():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true")
     ap.add_argument("--mcmc-steps", type=int, default=6000)
-    ap.add_argument("--mcmc-train", type=int, default=65536)
-    ap.add_argument("--mcmc-epochs", type=int, default=50)
+    ap.add_argument("--mcmc-train", type=int, default=131072)
+    ap.add_argument("--mcmc-epochs", type=int, default=100)
     ap.add_argument("--mcmc-nsub", type=int, default=40)
     ap.add_argument("--mcmc-stage1", default="hmc", choices=["hmc", "rwm"])
     return ap.parse_args()
