@@ -429,6 +429,10 @@ def run_gw(args, world, rank, local, dist):
         v, cores, n, dt = cpu_baseline(wl, args.config, args.cpu_seconds)
         cpu = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
                "sample": f"{n} full evaluations (K=1) of all {wl.n_events} events, {dt:.1f} s"}
+        # the same on one core (the reference's event loop split over threads
+        # scales with cores; the single-core rate shows the per-core cost)
+        v1, _, n1, dt1 = cpu_baseline(wl, args.config, max(1.0, args.cpu_seconds / 4), threads=1)
+        cpu["one_core"] = {"value": v1, "sample": f"{n1} full evaluations on 1 thread, {dt1:.1f} s"}
     c3 = None
     if rank == 0 and not args.no_variants:
         c3 = c3_sweep(local)
@@ -452,6 +456,7 @@ def run_gw(args, world, rank, local, dist):
                                         "min_blocks_per_sm": sfull[5] if sfull else None}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "binding": ("compute" if compute["frac"] and compute["frac"] > achieved / peak else "hbm"),
                          "kernel": (plain_name if K == 1 else ("k_multi" if shape[0] == 1 else "k_batched")),
                          "kernel_ms": kernel_ms,
                          "algorithmic_bytes_per_launch": alg, "compute": compute},
