@@ -101,6 +101,20 @@ __device__ __forceinline__ void issue_tile_hdr(const DevView& v, int tile, unsig
 // decoded, the type dispatched and the response clamp loaded once; the KR
 // evaluations are independent (instruction-level parallelism).
 // ---------------------------------------------------------------------------
+// Uniform-knot splines with stored slopes at KR points: in FP32 with an even
+// KR, pairs of points go through the packed-FP32 evaluator.
+template <typename T, bool catmull, int KR>
+__device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, const T (&x)[KR], bool trunc,
+                                                T (&val)[KR]) {
+  if constexpr (sizeof(T) == 4 && KR % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KR; j += 2) eval_prepared2<catmull>(d, n, x[j], x[j + 1], trunc, val[j], val[j + 1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < KR; ++j) val[j] = eval_prepared<T, catmull>(d, n, x[j], trunc);
+  }
+}
+
 template <typename T, int KR>
 __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const T* __restrict__ pl, int k0,
                                             int kstep, T (&val)[KR]) {
@@ -153,14 +167,10 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
 #pragma unroll
           for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, true>(d, n, x[j], trunc);
         } else {
-#pragma unroll
-          for (int j = 0; j < KR; ++j) val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
+          prepared_values<T, true, KR>(d, n, x, trunc, val);
         }
       } else if (type == kUniform) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          val[j] = eval_prepared<T, false>(d, n, x[j], trunc);
-        }
+        prepared_values<T, false, KR>(d, n, x, trunc, val);
       } else if (type == kGeneral) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
@@ -176,8 +186,7 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
 #pragma unroll
           for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, false>(d, n, x[j], trunc);
         } else {
-#pragma unroll
-          for (int j = 0; j < KR; ++j) val[j] = eval_prepared<T, true>(d, n, x[j], trunc);
+          prepared_values<T, true, KR>(d, n, x, trunc, val);
         }
       } else if (type == kBicubic) {
         const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;

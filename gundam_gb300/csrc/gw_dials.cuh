@@ -175,6 +175,91 @@ __device__ __forceinline__ T eval_knots(const T* __restrict__ d, int n, T x, boo
   return (hermite(p1, m1, p2, m2, fx));
 }
 
+// ---------------------------------------------------------------------------
+// Two FP32 evaluations in one instruction stream: sm_100+ packed FP32
+// arithmetic (add / sub / mul / fma .f32x2) on pairs held in one 64-bit
+// register.  Used where a thread evaluates one dial at two parameter points
+// (the batched kernel with two points per lane).
+// ---------------------------------------------------------------------------
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 add2_rm(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// eval_prepared at two points (FP32): the same interval, fraction and
+// end-slope rules; the Hermite cubic in the form p1 + fx(m1 + fx(B + fx A)),
+// A = m1 + m2 - 2(p2 - p1), B = 3(p2 - p1) - 2 m1 - m2.
+template <bool catmull>
+__device__ __forceinline__ void eval_prepared2(const float* __restrict__ d, int n, float xa, float xb, bool trunc,
+                                               float& va, float& vb) {
+  f32x2 xx = mul2(sub2(pk2(xa, xb), pk2(d[0], d[0])), pk2(d[1], d[1]));
+  const float nm2 = __int_as_float(0x4B000000 | (n - 2)) - 8388608.0f;  // (float)(n - 2)
+  float xa2, xb2;
+  if (trunc) {
+    upk2(xx, xa2, xb2);
+    xx = pk2(fminf(fmaxf(xa2, 0.0f), nm2 + 1.0f), fminf(fmaxf(xb2, 0.0f), nm2 + 1.0f));
+  }
+  const f32x2 magic = pk2(12582912.0f, 12582912.0f);
+  float fa, fb;
+  upk2(sub2(add2_rm(xx, magic), magic), fa, fb);
+  fa = fminf(fmaxf(fa, 0.0f), nm2);
+  fb = fminf(fmaxf(fb, 0.0f), nm2);
+  const f32x2 fi = pk2(fa, fb);
+  float ba, bb;
+  upk2(add2(fi, pk2(8388608.0f, 8388608.0f)), ba, bb);
+  const float* ka = d + 2 + 2 * (__float_as_int(ba) - 0x4B000000);
+  const float* kb = d + 2 + 2 * (__float_as_int(bb) - 0x4B000000);
+  const f32x2 fx = sub2(xx, fi);
+  const f32x2 p1 = pk2(ka[0], kb[0]);
+  const f32x2 p2 = pk2(ka[2], kb[2]);
+  const f32x2 dc = sub2(p2, p1);
+  float m1a = ka[1], m2a = ka[3], m1b = kb[1], m2b = kb[3];
+  if (catmull) {
+    float fxa, fxb, dca, dcb;
+    upk2(fx, fxa, fxb);
+    upk2(dc, dca, dcb);
+    if (fxa < 0.0f) m2a = dca;
+    if (fxa >= 1.0f) m1a = dca;
+    if (fxb < 0.0f) m2b = dcb;
+    if (fxb >= 1.0f) m1b = dcb;
+  }
+  const f32x2 m1 = pk2(m1a, m1b), m2 = pk2(m2a, m2b);
+  const f32x2 two = pk2(-2.0f, -2.0f);
+  const f32x2 a = add2(fma2(two, dc, m2), m1);
+  const f32x2 b = fma2(two, m1, sub2(mul2(pk2(3.0f, 3.0f), dc), m2));
+  upk2(fma2(fma2(fma2(a, fx, b), fx, m1), fx, p1), va, vb);
+}
+
 // Index of the facet for a value: BilinearIndex / BicubicIndex
 // (CalculateBilinearInterpolation.h:36-60), restricted to in-range reads.
 template <typename T>
