@@ -25,7 +25,6 @@ import os
 import time
 from pathlib import Path
 
-
 from .engine import Engine
 from .roofline import algorithmic_bytes
 from .workload import Workload
