@@ -104,3 +104,18 @@ def test_delayed_with_hmc_stage1_is_exact_with_a_biased_surrogate():
     p = mcmc.plain(f, np.tile(mean, (32, 1)), 600, mcmc.proposal_chol(cov), seed=5)
     assert d["stage2_accept"] > 0.99
     assert mcmc.ess(d["chains"], burn=60).min() > 5 * mcmc.ess(p["chains"], burn=60).min()
+
+
+def test_adaptive_pilot_learns_the_covariance_and_the_scale():
+    """Started from a proposal 10x too wide and uncorrelated, the pilot's
+    pooled covariance approaches the target's and its acceptance moves to
+    the 0.234 target."""
+    mean, cov, icov, f = _target(P=5, seed=3)
+    th0 = np.tile(mean, (32, 1)) + np.random.default_rng(4).normal(0, 0.1, (32, 5))
+    r = mcmc.adapt(f, th0, 10.0 * np.eye(5), cycles=6, steps=300, seed=5)
+    assert r["accept"][0] < 0.1
+    assert 0.15 < r["accept"][-1] < 0.35
+    np.testing.assert_allclose(np.sqrt(np.diag(r["cov"])), np.sqrt(np.diag(cov)), rtol=0.25)
+    corr = r["cov"] / np.sqrt(np.outer(np.diag(r["cov"]), np.diag(r["cov"])))
+    corr_t = cov / np.sqrt(np.outer(np.diag(cov), np.diag(cov)))
+    assert np.max(np.abs(corr - corr_t)) < 0.2
