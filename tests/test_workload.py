@@ -53,3 +53,22 @@ def test_mixed_has_every_dial_type_and_empty_bins():
     assert np.any(np.bincount(w.event_bin, minlength=w.n_bins) == 0)
     assert np.any(np.diff(w.event_dial_start) == 0)  # events without dials
     assert w.max_weight > 0 and w.n_tables == 2
+
+
+def test_c2_algorithmic_bytes_match_the_per_dial_estimate():
+    """The roofline numerator: the generated C2 mix stores ~15.35 reference
+    values per dial (0.5*9 + 0.2*24 + 0.1*32 + 0.1*10 + 0.05*37), so one K = 1
+    pass moves ~2.7 GB (FP32) / ~5.2 GB (FP64) at 5M events; the FP64 figure is
+    the FP32 one plus 4 bytes per stored value and per event weight."""
+    from gundam_gb300.roofline import algorithmic_bytes
+
+    w = Workload("c2", n_events=100000, seed=2)
+    lens = np.diff(w.dial_data_start)
+    assert abs(lens.sum() / w.n_dials - 15.35) < 0.1
+    b32, b64 = algorithmic_bytes(w, "fp32", 1), algorithmic_bytes(w, "fp64", 1)
+    assert b64 - b32 == 4 * int(lens.sum()) + 4 * w.n_events
+    per_event_scale = 5_000_000 / w.n_events
+    assert 2.6e9 < b32 * per_event_scale < 2.9e9
+    assert 5.0e9 < b64 * per_event_scale < 5.4e9
+    # K points add only their parameters in and their bin sums out
+    assert algorithmic_bytes(w, "fp32", 64) - b32 == 63 * (w.n_params * 8 + w.n_bins * 16)
