@@ -5,7 +5,8 @@
 * ``gundam_gb300/_lib/libgw_workload.so``  -- the synthetic workload generator.
 * ``oracle/_build/liboracle.so``           -- the CPU oracle (test infrastructure).
 * ``oracle/_ref/libref_dials.so``          -- the reference's own dial headers,
-  built only where the reference source tree is present (see oracle/ref/).
+  built only when the environment variable GUNDAM_REFERENCE names the
+  reference source tree (see oracle/ref/).
 
 The translation units compile in parallel; a full build takes well under a
 minute.  Nothing here links against torch.
@@ -87,10 +88,12 @@ def build(verbose: bool = False) -> dict[str, Path]:
              str(ORACLE / "oracle.cpp"), "-o", str(ORACLE / "_build" / "liboracle.so")],
         ),
     ]
+    # the reference's own sources, compiled into oracle/_ref/ as parity
+    # sources for the tests, only when GUNDAM_REFERENCE names their tree
     ref_script = ORACLE / "ref" / "build_ref.py"
-    reference = Path(os.environ.get("GUNDAM_REFERENCE", "/root/reference"))
-    if ref_script.exists() and (reference / "src" / "Utils" / "include").is_dir():
-        jobs.append(("ref_dials", [sys.executable, str(ref_script), str(reference)]))
+    reference = os.environ.get("GUNDAM_REFERENCE", "")
+    if reference and ref_script.exists() and (Path(reference) / "src" / "Utils" / "include").is_dir():
+        jobs.append(("ref_dials", [sys.executable, str(ref_script), reference]))
     _run_all(jobs, verbose)
     link = [
         nvcc, *ARCH, "-shared", "-cudart", "shared", *[str(o) for o in objs], "-o", str(LIBDIR / "libgw.so"),

@@ -55,7 +55,15 @@ class CacheManager:
     # ---- static control (CacheManager.h:62-135) ----
     @staticmethod
     def HasCUDA() -> bool:
-        return True
+        """Cache::Manager::HasCUDA: whether the library was built with CUDA
+        (CacheManager.cpp:190-192); False when libgw cannot be loaded."""
+        try:
+            lib = N.libgw()
+        except (OSError, RuntimeError):
+            return False
+        v = C.c_int32()
+        N.check(lib.gw_using_cuda(C.byref(v)))
+        return bool(v.value)
 
     @staticmethod
     def HasGPU(dump: bool = False) -> bool:

@@ -125,6 +125,13 @@ struct gw_engine {
   std::vector<int32_t> sorted_to_result;
   gw_layout_info layout{};
   int64_t resident = 0;
+  // Every launch chain uses the engine's one set of scratch arrays (mirrored
+  // parameters, penalty, partial sums, likelihood counters, status word), so
+  // chains on different streams are ordered by an event recorded at the end
+  // of each chain (chain_begin / chain_end).
+  cudaEvent_t chain_done = nullptr;
+  cudaStream_t chain_stream = nullptr;  // stream of the last chain; nullptr: none yet
+  bool chain_any = false;
   // profiling
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
@@ -137,6 +144,7 @@ struct gw_engine {
       cudaEventDestroy(pe.first);
       cudaEventDestroy(pe.second);
     }
+    if (chain_done) cudaEventDestroy(chain_done);
     for (void* p : dev_allocs) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -168,6 +176,33 @@ static int fail(gw_engine* e, int code, const char* fmt, ...) {
     if (!(e)) return GW_ERR_ARG;                                                \
     if ((e)->initialized) return fail((e), GW_ERR_STATE, "engine already initialized"); \
   } while (0)
+
+// Cross-stream ordering of the engine's launch chains.  Every chain reads and
+// writes the engine's one set of scratch arrays, so a chain (or a copy into
+// the engine's tables or data) on stream s first waits for the last chain,
+// whichever stream that ran on, and each chain records chain_done on its
+// stream when its launches are queued.  Nothing is waited on or recorded
+// while s is being captured into a caller's graph: a captured wait on an
+// event recorded outside the capture is not allowed, so a caller that
+// captures engine calls orders its streams itself.
+static int chain_begin(gw_engine* e, cudaStream_t s) {
+  if (!e->chain_any || e->chain_stream == s) return GW_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GW_CUDA(e, cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return GW_OK;
+  GW_CUDA(e, cudaStreamWaitEvent(s, e->chain_done, 0));
+  return GW_OK;
+}
+
+static int chain_end(gw_engine* e, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GW_CUDA(e, cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return GW_OK;
+  GW_CUDA(e, cudaEventRecord(e->chain_done, s));
+  e->chain_stream = s;
+  e->chain_any = true;
+  return GW_OK;
+}
 
 static bool par_ok(const gw_engine* e, int32_t p) { return p >= 0 && p < e->cfg.n_params; }
 static bool res_ok(const gw_engine* e, int32_t r) { return r >= 0 && r < e->cfg.n_results; }
@@ -465,6 +500,8 @@ extern "C" int gw_set_data(gw_engine* e, const double* data, int32_t n_bins) {
   std::memcpy(e->data.data(), data, sizeof(double) * (size_t)n_bins);
   if (e->initialized) {
     GW_CUDA(e, cudaSetDevice(e->device));
+    const int rc = chain_begin(e, e->stream);  // a chain on another stream may still read the data
+    if (rc) return rc;
     GW_CUDA(e, cudaMemcpyAsync((void*)e->view.data, data, sizeof(double) * (size_t)n_bins, cudaMemcpyHostToDevice,
                                e->stream));
     GW_CUDA(e, cudaStreamSynchronize(e->stream));
@@ -912,6 +949,7 @@ int build_and_upload(gw_engine* e) {
   GW_CUDA(e, cudaSetDevice(e->device));
   GW_CUDA(e, cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device));
   GW_CUDA(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  GW_CUDA(e, cudaEventCreateWithFlags(&e->chain_done, cudaEventDisableTiming));
   e->kpad = ((e->cfg.k_max + 63) / 64) * 64;  // a batched pass covers up to 64 points
   const int P = e->cfg.n_params;
   const int kpad = e->kpad;
@@ -1153,6 +1191,10 @@ static int refresh_tables(gw_engine* e) {
   bool copied = false;
   for (HostTable& h : e->tables) {
     if (!h.has_fn && h.dirty) {
+      if (!copied) {
+        const int rc = chain_begin(e, e->stream);  // a chain on another stream may still read the table
+        if (rc) return rc;
+      }
       unsigned char* dst = (unsigned char*)e->view.table_arena + off * tsz;
       if (tsz == 8) {
         GW_CUDA(e, cudaMemcpyAsync(dst, h.values.data(), sizeof(double) * h.size, cudaMemcpyHostToDevice,
@@ -1242,6 +1284,8 @@ extern "C" int gw_eval(gw_engine* e, const double* params, int32_t K, double* su
                                s));
     return GW_OK;
   };
+  rc = chain_begin(e, s);
+  if (rc) return rc;
   if (e->use_graph) {
     auto it = e->graphs.find(K);
     if (it == e->graphs.end()) {
@@ -1265,6 +1309,8 @@ extern "C" int gw_eval(gw_engine* e, const double* params, int32_t K, double* su
     rc = run();
     if (rc) return rc;
   }
+  rc = chain_end(e, s);
+  if (rc) return rc;
   rc = check_status(e);  // synchronizes the stream
   if (rc) return rc;
   if (sums) std::memcpy(sums, e->h_sums.p, sizeof(double) * (size_t)K * B);
@@ -1284,6 +1330,8 @@ extern "C" int gw_eval_device(gw_engine* e, const double* d_params, int32_t K, d
   int rc = refresh_tables(e);
   if (rc) return rc;
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  rc = chain_begin(e, s);
+  if (rc) return rc;
   if (e->use_graph) {
     // the launch chain captured once per (K, pointers, stream) and replayed
     const std::vector<uintptr_t> key = {(uintptr_t)K,       (uintptr_t)d_params, (uintptr_t)d_sums,
@@ -1310,6 +1358,7 @@ extern "C" int gw_eval_device(gw_engine* e, const double* d_params, int32_t K, d
   } else {
     rc = launch_chain(e, d_params, K, d_sums, d_sums2, d_llh, d_llh_stat, s);
   }
+  if (rc == GW_OK) rc = chain_end(e, s);
   if (rc == GW_OK) e->weights_valid = e->copy_weights && K == 1;
   return rc;
 }
@@ -1330,6 +1379,7 @@ extern "C" int gw_use_graph(gw_engine* e, int32_t on) {
 
 // K = 1: times both K = 1 kernels and keeps the faster.
 static int autotune_plain(gw_engine* e) {
+  GW_CUDA(e, cudaDeviceSynchronize());  // every earlier chain, whichever stream
   std::vector<double> pts((size_t)e->cfg.n_params);
   for (size_t i = 0; i < pts.size(); ++i) pts[i] = 0.001 * (double)((i * 7919) % 17) - 0.008;
   GW_CUDA(e, cudaMemcpy(e->d_params, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice));
@@ -1374,6 +1424,7 @@ extern "C" int gw_autotune(gw_engine* e, int32_t K) {
   }
   if (K < 1 || K > e->cfg.k_max) return fail(e, GW_ERR_ARG, "autotune needs 1 <= K <= k_max");
   GW_CUDA(e, cudaSetDevice(e->device));
+  GW_CUDA(e, cudaDeviceSynchronize());  // every earlier chain, whichever stream
   // deterministic synthetic points: all parameters at 0 except tiny offsets
   std::vector<double> pts((size_t)K * e->cfg.n_params);
   for (size_t i = 0; i < pts.size(); ++i) pts[i] = 0.001 * (double)((i * 7919) % 17) - 0.008;
@@ -1532,6 +1583,7 @@ extern "C" int gw_get_event_weights(gw_engine* e, double* w) {
   if (!e->weights_valid) return fail(e, GW_ERR_STATE, "no event weights: enable the copy and evaluate with K=1");
   GW_CUDA(e, cudaSetDevice(e->device));
   GW_CUDA(e, cudaStreamSynchronize(e->stream));
+  if (e->chain_any) GW_CUDA(e, cudaEventSynchronize(e->chain_done));  // the chain that wrote them, any stream
   GW_CUDA(e, cudaMemcpy(w, e->d_evw, sizeof(double) * (size_t)e->cfg.n_results, cudaMemcpyDeviceToHost));
   return GW_OK;
 }

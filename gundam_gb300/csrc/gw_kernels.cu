@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 // before a payload stage is refilled, RED among the reducers.  Every CTA runs
 // the same number of iterations on both sides, so the hand-over cannot
 // deadlock; a timed-out copy marks the block failed and the protocol runs on
-// without work.
+// without work: no further copy is issued, no header is decoded, and before
+// the CTA exits thread 0 waits (bounded) for every copy still in flight.
 // ---------------------------------------------------------------------------
 constexpr int kWsEval = 192, kWsRed = 64;
 constexpr int kBarEval = 1, kBarFull = 2, kBarEmpty = 4, kBarRed = 6;
@@ -281,14 +282,23 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
     int nd = 0, nd_next = 0;
     if (ntile > 0) nd = v.tiles[blockIdx.x].ndials;
     if (ntile > 1) nd_next = v.tiles[blockIdx.x + gridDim.x].ndials;
+    // thread 0: iteration whose copy was last issued into each stage and not
+    // yet seen complete (-1: none)
+    int pend0 = ntile > 0 ? 0 : -1, pend1 = ntile > 1 ? 1 : -1;
     for (int it = 0; it < ntile; ++it) {
       const int tile = blockIdx.x + it * gridDim.x;
       const int st = it & 1;
       const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)((it >> 1) & 1), kWaitLimitNs);
       if (!ok) s_fail = 1;
+      if (tid == 0 && ok) {
+        if (st) pend1 = -1;
+        else pend0 = -1;
+      }
       if (it >= 2) named_sync(kBarEmpty + st, kPlainThreads);  // the reducers are done with buffer st
       T* dv = dval + st * 1024;
-      if (ok) {
+      // after any failed wait the stages hold nothing trustworthy: headers
+      // are not decoded, so no shared-memory index comes from them
+      if (ok && !s_fail) {
         const T* pl = (const T*)(smem + st * TB);
         const uint64_t* hs = shdr + st * hstride;
         for (int i = tid; i < nd; i += kWsEval) {
@@ -303,9 +313,23 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
         nd = nd_next;
         if (it + 2 < ntile) nd_next = v.tiles[tile + 2 * gridDim.x].ndials;
       }
-      named_sync(kBarEval, kWsEval);  // stage st (payload and headers) fully read
-      if (tid == 0 && it + 2 < ntile)
+      named_sync(kBarEval, kWsEval);  // stage st (payload and headers) fully read; s_fail visible
+      // after a failed wait no further copy is issued: a stage whose copy
+      // timed out may still be written by it
+      if (tid == 0 && it + 2 < ntile && !s_fail) {
         issue_tile_hdr(v, tile + 2 * gridDim.x, smem + st * TB, shdr + st * hstride, &bar[st]);
+        if (st) pend1 = it + 2;
+        else pend0 = it + 2;
+      }
+    }
+    // the reducers' last two EMPTY arrivals, so every named-barrier phase
+    // gets its full count of threads
+    for (int j = ntile >= 2 ? ntile - 2 : 0; j < ntile; ++j) named_sync(kBarEmpty + (j & 1), kPlainThreads);
+    // after a failure, wait (bounded) for every copy still in flight before
+    // the CTA's shared memory is released
+    if (tid == 0 && s_fail) {
+      if (pend0 >= 0) mbar_wait_bounded(&bar[0], (uint32_t)((pend0 >> 1) & 1), kWaitLimitNs);
+      if (pend1 >= 0) mbar_wait_bounded(&bar[1], (uint32_t)((pend1 >> 1) & 1), kWaitLimitNs);
     }
   } else {
     const int r = tid - kWsEval;
@@ -580,6 +604,17 @@ cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2
 }
 
 }  // namespace gw
+
+// Compiled by the CUDA compiler: the device code above is in this library.
+extern "C" int gw_using_cuda(int32_t* using_cuda) {
+  if (!using_cuda) return GW_ERR_ARG;
+#ifdef __CUDACC__
+  *using_cuda = 1;
+#else
+  *using_cuda = 0;
+#endif
+  return GW_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Failure-path self-test: an mbarrier that expects bytes no copy will ever

@@ -25,8 +25,12 @@
 //    kernel.  Calls whose work overlaps on the GPU (different streams, or a
 //    second host thread) race on the array; serialise them.
 //  * The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current and caches it; make
-//    that first call before any stream capture.
+//    (cudaGetSymbolAddress) with that device current and caches it for the
+//    rest of the process; make that first call before any stream capture.
+//    The address belongs to the device's primary context: cudaDeviceReset
+//    destroys that context (the module is loaded again, possibly elsewhere),
+//    so the cached address is stale after a reset and the entry point must
+//    not be called on that device again in the same process.
 #include <mutex>
 
 #include "gw.h"

@@ -197,16 +197,23 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
     # both samplers start from the same states, taken after a delayed-
     # acceptance warm-up (it mixes fastest) so that neither starts out of
     # equilibrium; the first burn_frac of each run is discarded as well
+    # The fall-back to plain steps is decided in the warm-up alone and frozen
+    # for the recorded run: a switch that depends on the recorded chain's own
+    # history would make the recorded sampler adaptive.  A warm-up that fell
+    # back makes the recorded delayed-acceptance arm plain from its first step.
     t0 = time.perf_counter()
+    warm_fell_back = None
     if warm_steps > 0:
         w = mcmc.delayed(f_exact, f_sur, th0, warm_steps, L, n_sub=n_sub, seed=seed + 3, max_error=max_error,
                          stage1=stage1_of(sur), record=False)
         th0 = w["final"]
+        warm_fell_back = w["fell_back_at_step"]
     t_warm = time.perf_counter() - t0
+    frozen = dict(max_error=float("inf"), start_plain=warm_fell_back is not None)
     p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7, thin=thin)
-    d = mcmc.delayed(f_exact, f_sur, th0, da_steps, L, n_sub=n_sub, seed=seed + 8, max_error=max_error,
-                     stage1=stage1_of(sur), thin=thin)
-    dl = mcmc.delayed(f_exact, None, th0, da_steps, L, n_sub=n_sub, seed=seed + 9, max_error=max_error,
+    d = mcmc.delayed(f_exact, f_sur, th0, da_steps, L, n_sub=n_sub, seed=seed + 8, stage1=stage1_of(sur),
+                     thin=thin, **frozen)
+    dl = mcmc.delayed(f_exact, None, th0, da_steps, L, n_sub=n_sub, seed=seed + 9, max_error=float("inf"),
                       stage1=stage1_of(lin), thin=thin) if lin else None
     bp = int(burn_frac * p["chains"].shape[0])
     bd = int(burn_frac * d["chains"].shape[0])
@@ -226,6 +233,8 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
         "workload": f"{config}: {wl.n_events} events, {wl.n_dials} dials, {B} bins, {P} params",
         "precision": precision, "chains": chains, "plain_steps": steps, "delayed_steps": da_steps, "n_sub": n_sub,
         "thin": thin, "warm_steps": warm_steps, "warm_seconds": t_warm, "burn_fraction": burn_frac,
+        "fallback": {"decided_in": "warm-up", "warm_up_fell_back_at_step": warm_fell_back,
+                     "recorded_run_plain_from_start": warm_fell_back is not None},
         "fit": {"f": fr["f"], "iterations": fr["iterations"], "seconds": fr["seconds"]},
         "pilot": {"proposal": proposal, "seconds": t_adapt, "scale": scale,
                   "accept": ad["accept"] if proposal == "adapted" else None,

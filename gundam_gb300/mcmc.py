@@ -138,16 +138,22 @@ def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1):
 
 
 def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0, record=True, stage1=None,
-            thin=1):
+            thin=1, start_plain=False):
     """stage1: optional callable (theta, fs, n_sub, seed) -> (phi, fphi, n_acc)
     that runs the surrogate sub-chains elsewhere (on the device, with the
     same proposal L and its own random numbers); fs None asks for the
-    surrogate values at theta.  Without it the sub-chains run here on f_sur."""
+    surrogate values at theta.  Without it the sub-chains run here on f_sur.
+    The run falls back to plain steps for good once the running mean of the
+    stage-2 error |df - df_s| exceeds max_error (inf: never); start_plain
+    runs plain steps from the first one (a fall-back decided elsewhere)."""
     rng = np.random.default_rng(seed)
     th = np.array(theta0, dtype=np.float64)
     C, P = th.shape
     f = f_exact(th)
-    fs = stage1(th, None, 0, seed)[1] if stage1 else f_sur(th)
+    if start_plain:
+        fs = np.full(C, np.nan)
+    else:
+        fs = stage1(th, None, 0, seed)[1] if stage1 else f_sur(th)
     out = np.empty((n_steps // thin, C, P)) if record else None
 
     def keep(s):
@@ -157,7 +163,7 @@ def delayed(f_exact, f_sur, theta0, n_steps, L, n_sub=10, seed=0, max_error=20.0
     n_exact = C
     n_sur = C
     err_hist = []
-    fell_back_at = None
+    fell_back_at = 0 if start_plain else None
     t0 = time.perf_counter()
     for s in range(n_steps):
         if fell_back_at is not None:

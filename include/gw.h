@@ -114,6 +114,12 @@ typedef struct gw_config {
 
 /* ---- engine lifetime --------------------------------------------------- */
 
+/* Cache::Manager::HasCUDA -> Cache::Parameters::UsingCUDA
+ * (CacheManager.cpp:190-192; CacheParameters.cpp:12-18): writes 1 when the
+ * library's kernels were compiled by the CUDA compiler (always, for libgw),
+ * else 0.  Needs no device. */
+int gw_using_cuda(int32_t* using_cuda);
+
 /* Cache::Manager::HasGPU (CacheManager.h:78; CacheParameters.cpp:24-79).
  * Writes 1 when a usable CUDA device exists, else 0. */
 int gw_has_gpu(int32_t* has_gpu);
@@ -229,7 +235,13 @@ int gw_eval(gw_engine* e, const double* params, int32_t K, double* sums, double*
             double* llh, double* llh_stat);
 
 /* Same as gw_eval with DEVICE pointers, asynchronous on `stream`
- * (a cudaStream_t; NULL = the engine's own stream).  Any output may be NULL. */
+ * (a cudaStream_t; NULL = the engine's own stream).  Any output may be NULL.
+ * All evaluations of one engine share its scratch arrays, so the engine
+ * orders them on the GPU: each call's launches wait for the previous call's,
+ * whichever stream that used (gw_eval included), through an event recorded
+ * at the end of every call.  While `stream` is being captured into the
+ * caller's own CUDA graph no such wait or record is added; the caller then
+ * orders the captured work against other calls on the engine itself. */
 int gw_eval_device(gw_engine* e, const double* d_params, int32_t K, double* d_sums,
                    double* d_sums2, double* d_llh, double* d_llh_stat, void* stream);
 
@@ -306,8 +318,11 @@ int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weights_launches,
  * fixed array inside the library (65536 block partials + 4096 counters, about
  * 528 KiB per GPU, held until exit): K <= 4096 and K * ceil(n_bins/256) <=
  * 65536, else GW_ERR_LIMIT.  All calls share that array: calls that overlap on
- * the GPU race.  The first call on a device looks up the array's address; make
- * it before any stream capture.  Asynchronous on `stream`. */
+ * the GPU race.  The first call on a device looks up the array's address and
+ * keeps it for the rest of the process; make it before any stream capture.
+ * cudaDeviceReset destroys the context that address belongs to, so do not
+ * call this on a device after a reset of that device in the same process.
+ * Asynchronous on `stream`. */
 int gw_llh_noalloc(const double* d_sums, const double* d_sums2, const double* d_data, int32_t n_bins, int32_t K,
                    int32_t llh_type, double* d_llh, void* stream);
 

@@ -39,4 +39,6 @@ def main(reference: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python oracle/ref/build_ref.py <path of the GUNDAM source tree>")
+    main(sys.argv[1])

@@ -44,3 +44,17 @@ def test_has_gpu_reports_the_host():
     import torch
 
     assert CacheManager.HasGPU() == torch.cuda.is_available()
+
+
+def test_has_cuda_asks_the_library():
+    """HasCUDA reports whether the kernels were compiled with CUDA
+    (Cache::Parameters::UsingCUDA, CacheParameters.cpp:12-18): the library
+    answers, no device is needed."""
+    import ctypes as C
+
+    from gundam_gb300 import _native as N
+
+    v = C.c_int32(-1)
+    assert N.libgw().gw_using_cuda(C.byref(v)) == N.GW_OK
+    assert v.value == 1
+    assert CacheManager.HasCUDA() is True

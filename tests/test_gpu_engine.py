@@ -66,3 +66,43 @@ def test_bounded_wait_gives_up_and_reports():
     s, s2, l, st = eng.eval(wl.nominal())
     assert np.isfinite(l[0])
     eng.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_device_and_host_evaluations_on_two_streams_are_ordered(graph):
+    """gw_eval_device on a caller stream followed at once, with no host
+    synchronisation, by gw_eval on the engine's stream (and the reverse): both
+    use the engine's one set of scratch arrays, so the engine must order them.
+    Each result is checked against the oracle."""
+    torch = pytest.importorskip("torch")
+    wl = Workload("c1", seed=12)
+    orc = Oracle(wl, llh_type=N.GW_LLH_POISSON)
+    K = 8
+    eng = Engine.from_workload(wl, precision="fp64", k_max=K, llh_type=N.GW_LLH_POISSON)
+    eng.use_graph(graph)
+    pa = wl.draw_points(K, 21)
+    pb = wl.draw_points(K, 22)
+    ref_a, ref_b = orc.eval(pa), orc.eval(pb)
+    d_p = torch.from_numpy(pa).cuda()
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for rep in range(3):
+        d_s = torch.full((K, wl.n_bins), float("nan"), dtype=torch.float64, device="cuda")
+        d_s2 = torch.full_like(d_s, float("nan"))
+        d_l = torch.full((K,), float("nan"), dtype=torch.float64, device="cuda")
+        d_st = torch.full_like(d_l, float("nan"))
+        torch.cuda.synchronize()
+        eng.eval_device(d_p.data_ptr(), K, d_s.data_ptr(), d_s2.data_ptr(), d_l.data_ptr(), d_st.data_ptr(),
+                        stream.cuda_stream)
+        sums, sums2, llh, stat = eng.eval(pb)  # engine stream, no host sync in between
+        eng.eval_device(d_p.data_ptr(), K, d_s.data_ptr(), d_s2.data_ptr(), d_l.data_ptr(), d_st.data_ptr(),
+                        stream.cuda_stream)
+        stream.synchronize()
+        eng.sync()
+        assert _rel(sums, ref_b["sums"]) <= 1e-12, rep
+        assert _rel(sums2, ref_b["sums2"]) <= 1e-12, rep
+        assert np.max(np.abs(llh - ref_b["llh"])) <= 1e-6, rep
+        assert _rel(d_s.cpu().numpy(), ref_a["sums"]) <= 1e-12, rep
+        assert _rel(d_s2.cpu().numpy(), ref_a["sums2"]) <= 1e-12, rep
+        assert np.max(np.abs(d_l.cpu().numpy() - ref_a["llh"])) <= 1e-6, rep
+    eng.close()

@@ -69,6 +69,25 @@ def test_fallback_when_surrogate_error_grows():
     assert r["fell_back_at_step"] is not None
 
 
+def test_frozen_fallback_runs_plain_from_the_first_step_or_never_switches():
+    """The fall-back decided in a warm-up is frozen for the recorded run:
+    start_plain makes every step a plain step (the surrogate is never
+    called), max_error = inf never switches whatever the error."""
+    mean, cov, icov, f = _target()
+    L = mcmc.proposal_chol(cov)
+
+    def never(th):
+        raise AssertionError("surrogate called in a plain run")
+    r = mcmc.delayed(f, never, np.tile(mean, (8, 1)), 50, L, n_sub=4, seed=5, start_plain=True)
+    assert r["fell_back_at_step"] == 0 and r["n_surrogate"] == 8
+    noise = np.random.default_rng(9)
+
+    def bad(th):
+        return f(th) + noise.normal(0.0, 10.0, th.shape[0])
+    r = mcmc.delayed(f, bad, np.tile(mean, (16, 1)), 200, L, n_sub=4, seed=5, max_error=float("inf"))
+    assert r["fell_back_at_step"] is None
+
+
 def test_ess_of_independent_draws_is_close_to_n():
     rng = np.random.default_rng(0)
     x = rng.standard_normal((4000, 4, 3))

@@ -66,3 +66,35 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     # 300 points x 256 blocks of bins exceed the 65536 block partials
     rc = lib.gw_llh_noalloc(_vp(d), _vp(d), _vp(d), 256 * 256, 300, N.GW_LLH_POISSON, _vp(d), None)
     assert rc == N.GW_ERR_LIMIT
+
+
+def test_noalloc_request_exactly_at_the_bound():
+    """K * ceil(n_bins / 256) == 65536 exactly (256 points of 65536 bins): the
+    last block partial lands at the end of the array, next to the counters.
+    Accepted, and equal to a host sum of the same per-bin Poisson terms, on
+    two calls in a row."""
+    torch = pytest.importorskip("torch")
+    import math
+
+    K, B = 256, 65536
+    rng = np.random.default_rng(17)
+    sums = rng.uniform(0.5, 40.0, size=(K, B))
+    data = rng.poisson(sums[0]).astype(np.float64)
+    ref = []
+    for k in range(K):
+        p = sums[k]
+        term = np.where(data <= 0.0, 2.0 * p, 2.0 * (p - data + data * np.log(np.where(data > 0, data, 1.0) / p)))
+        ref.append(math.fsum(term.tolist()))
+    ref = np.array(ref)
+    d_s = torch.from_numpy(sums).cuda()
+    d_s2 = torch.from_numpy(sums * 0.01).cuda()
+    d_data = torch.from_numpy(data).cuda()
+    lib = N.libgw()
+    for call in range(2):
+        out = torch.full((K,), float("nan"), dtype=torch.float64, device="cuda")
+        rc = lib.gw_llh_noalloc(_vp(d_s), _vp(d_s2), _vp(d_data), B, K, N.GW_LLH_POISSON, _vp(out), None)
+        assert rc == N.GW_OK, N.last_error(None)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.all(np.isfinite(got)), f"call {call}"
+        assert np.max(np.abs(got - ref)) <= LLH_ABS, f"call {call}"
