@@ -73,7 +73,7 @@ def build(verbose: bool = False) -> dict[str, Path]:
     cxx = os.environ.get("CXX", "g++")
 
     common_nv = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
-    units = ["gw_kernels.cu", "gw_lanes.cu", "gw_multi.cu", "gw_noalloc.cu", "gw_mlp.cu", "gw_engine.cpp"]
+    units = ["gw_kernels.cu", "gw_lanes.cu", "gw_multi.cu", "gw_ws.cu", "gw_noalloc.cu", "gw_mlp.cu", "gw_engine.cpp"]
     objs = [objdir / (Path(u).stem + ".o") for u in units]
     jobs = [(u, [nvcc, *common_nv, "-c", str(CSRC / u), "-o", str(o)]) for u, o in zip(units, objs)]
     jobs += [

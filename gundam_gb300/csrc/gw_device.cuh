@@ -74,6 +74,15 @@ __device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit
 
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per tile copy
 
+// Named barriers of warp-specialised kernels: `count` threads (a multiple of
+// 32) complete a phase; arrive does not wait, sync does.
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 // Thread 0: start the bulk copy of a tile's payload into a stage buffer.
 __device__ __forceinline__ void issue_tile(const DevView& v, int tile, unsigned char* buf, uint64_t* bar) {
   const TileDesc td = v.tiles[tile];
@@ -115,7 +124,38 @@ __device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, 
   }
 }
 
-template <typename T, int KR>
+// The KR values of one parameter at points k0, k0 + kstep, ...  With VX the
+// points are contiguous (kstep == 1) and k0 * sizeof(T) is a multiple of 16,
+// so whole 16-byte vectors are loaded.
+template <typename T, int KR, bool VX>
+__device__ __forceinline__ void load_points(const T* __restrict__ p, int kstep, T (&x)[KR]) {
+  if constexpr (VX && (KR * sizeof(T)) % 16 == 0) {
+    if constexpr (sizeof(T) == 4) {
+      const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+      for (int i = 0; i < KR / 4; ++i) {
+        const float4 f = q[i];
+        x[4 * i] = f.x;
+        x[4 * i + 1] = f.y;
+        x[4 * i + 2] = f.z;
+        x[4 * i + 3] = f.w;
+      }
+    } else {
+      const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+      for (int i = 0; i < KR / 2; ++i) {
+        const double2 f = q[i];
+        x[2 * i] = f.x;
+        x[2 * i + 1] = f.y;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < KR; ++j) x[j] = p[j * kstep];
+  }
+}
+
+template <typename T, int KR, bool VX = false>
 __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const T* __restrict__ pl, int k0,
                                             int kstep, T (&val)[KR]) {
   const int type = hdr_type(h);
@@ -151,8 +191,7 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
     hi = c.y;
     const bool trunc = (v.pflags[p0] & 1) != 0;
     T x[KR];
-#pragma unroll
-    for (int j = 0; j < KR; ++j) x[j] = xs[j * kstep];
+    load_points<T, KR, VX>(xs, kstep, x);
     if (type == kNorm) {
 #pragma unroll
       for (int j = 0; j < KR; ++j) val[j] = x[j];
@@ -178,9 +217,10 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_graph<T>(d, n, x[j], trunc);
       } else if (type == kBilinear) {
-        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+        T y[KR];
+        load_points<T, KR, VX>((const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0, kstep, y);
 #pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], ys[j * kstep], trunc);
+        for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], y[j], trunc);
       } else if (type == kCompact) {
         if (v.spline_knots) {
 #pragma unroll
@@ -189,9 +229,10 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
           prepared_values<T, true, KR>(d, n, x, trunc, val);
         }
       } else if (type == kBicubic) {
-        const T* ys = (const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0;
+        T y[KR];
+        load_points<T, KR, VX>((const T*)v.x + (size_t)hdr_p1(h) * v.kpad + k0, kstep, y);
 #pragma unroll
-        for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], ys[j * kstep], trunc);
+        for (int j = 0; j < KR; ++j) val[j] = eval_bicubic<T>(d, x[j], y[j], trunc);
       } else {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = T(1);
@@ -243,6 +284,17 @@ __device__ __forceinline__ double llh_bb_oa2021(double data, double pred, double
     stat = mc - data + data * (log(data) - log(mc));
   }
   return 2.0 * stat + 2.0 * penalty;
+}
+
+// One Barlow-Beeston bin from the histogram's (sum of w, sqrt of sum of w^2),
+// as BarlowBeestonBanff2022::eval(const SamplePair&, int) takes it
+// (BarlowBeestonBanff2022.h:92-148): the stored sqrt squared again, and +inf
+// for a non-finite value (the reference's throwIfInfLlh = false branch).
+__device__ __forceinline__ double llh_bb_bin(double data, double pred, double sqrt_sum_w2) {
+  double mcuncert = sqrt_sum_w2;
+  mcuncert *= mcuncert;
+  if (!isfinite(mcuncert) || mcuncert < 0.0) return HUGE_VAL;
+  return llh_bb_oa2021(data, pred, mcuncert);
 }
 
 }  // namespace

@@ -75,7 +75,9 @@ cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
 // Shape of a batched (K > 1) launch.  kind 0 = k_batched: lanes over points,
 // kc points per warp pass, kr points per lane.  kind 1 = k_multi: threads over
-// dials, kc points per chunk, kr points per thread.  threads per block and
+// dials, kc points per chunk, kr points per thread.  kind 3 = k_ws: the
+// warp-specialised K = 1 kernel with kc = kr points per evaluator thread.
+// threads per block and
 // payload stages for both; minb = CTAs per SM the kernel's register
 // allocation targets (its launch bounds; 0 = the compiler's choice).
 struct BatchedShape {
@@ -93,6 +95,10 @@ struct ShapeEntry {
 };
 int lane_shapes(const ShapeEntry** out);   // gw_lanes.cu
 int multi_shapes(const ShapeEntry** out);  // gw_multi.cu
+// kind 3 = k_ws (gw_ws.cu): the warp-specialised K = 1 kernel with kc points
+// per evaluator thread (kr = kc).
+int ws_shapes(const ShapeEntry** out);
+size_t ws_smem_bytes(const DevView& v, int kc);
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s);
 // True when every pass of the shape over K points stays inside the kpad
 // columns of the parameter and partial-sum arrays.

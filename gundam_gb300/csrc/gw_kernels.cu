@@ -242,12 +242,6 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 constexpr int kWsEval = 192, kWsRed = 64;
 constexpr int kBarEval = 1, kBarFull = 2, kBarEmpty = 4, kBarRed = 6;
 
-__device__ __forceinline__ void named_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ void named_arrive(int id, int count) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain_ws(const DevView v) {
@@ -410,8 +404,7 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
     if (v.llh_type == 1) {
       term = llh_poisson(v.data[b], s);
     } else if (v.llh_type == 2) {
-      const double err = sqrt(s2);  // BinContent::sqrtSumSqWeights, squared again by the LLH
-      term = llh_bb_oa2021(v.data[b], s, err * err);
+      term = llh_bb_bin(v.data[b], s, sqrt(s2));  // BinContent::sqrtSumSqWeights, squared again by the LLH
     }
   }
   if (v.llh_type == 0 || (llh == nullptr && llh_stat == nullptr)) return;
@@ -463,6 +456,7 @@ size_t plain_smem_bytes(const DevView& v) {
 
 size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
   const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  if (b.kind == 3) return ws_smem_bytes(v, b.kc);  // k_ws
   if (b.kind == 1) {  // k_multi
     return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
            (size_t)kMaxTileEvents * b.kc * sizeof(double) + (size_t)1024 * b.kc * tsz + kMaxTileEvents * tsz +
@@ -479,20 +473,25 @@ static const void* plain_fn(int kind) {
   return kind == 1 ? (const void*)k_plain_ws<T> : (const void*)k_plain<T>;
 }
 
-// Every batched shape: the lanes-over-points family (gw_lanes.cu), then the
-// dials-over-threads family (gw_multi.cu).
+// Every batched shape: the lanes-over-points family (gw_lanes.cu), the
+// dials-over-threads family (gw_multi.cu), then the warp-specialised small-K
+// family (gw_ws.cu).
 static const ShapeEntry* shape_entry(int i) {
   const ShapeEntry* lanes;
   const ShapeEntry* multi;
+  const ShapeEntry* ws;
   const int nl = lane_shapes(&lanes);
   const int nm = multi_shapes(&multi);
-  if (i < 0 || i >= nl + nm) return nullptr;
-  return i < nl ? &lanes[i] : &multi[i - nl];
+  const int ns = ws_shapes(&ws);
+  if (i < 0 || i >= nl + nm + ns) return nullptr;
+  if (i < nl) return &lanes[i];
+  if (i < nl + nm) return &multi[i - nl];
+  return &ws[i - nl - nm];
 }
 
 int batched_shape_count() {
   const ShapeEntry* p;
-  return lane_shapes(&p) + multi_shapes(&p);
+  return lane_shapes(&p) + multi_shapes(&p) + ws_shapes(&p);
 }
 
 BatchedShape batched_shape(int i) {

@@ -66,8 +66,7 @@ __global__ void __launch_bounds__(256) k_llh_noalloc(const double* __restrict__ 
     if (llh_type == GW_LLH_POISSON) {
       term = llh_poisson(data[b], s);
     } else {
-      const double err = sqrt(s2);
-      term = llh_bb_oa2021(data[b], s, err * err);
+      term = llh_bb_bin(data[b], s, sqrt(s2));
     }
   }
   __shared__ double red[32];

@@ -1,15 +1,16 @@
 """A small, self-contained case for profiling one kernel under ncu.
 
-    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64} [n_events] [shape_index]
+    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64} [n_events] [shape_index] [K]
     python -m gundam_gb300.profile_case train [steps]
     python -m gundam_gb300.profile_case substeps [n_sub]
 
 plain / batched: builds the C2-shaped workload with n_events events (default
 1,000,000: a payload above the 129 MB L2 but a few GB of device memory at
 most) and evaluates it four times: K = 1 (the K = 1 kernel, on a K = 1
-engine: Catmull-Rom splines stored as knot values in FP32) or K = 64 with
-batched shape `shape_index` (an entry of Engine.compiled_shapes(); without
-it the autotuner picks one first, and the chosen index is printed).
+engine: Catmull-Rom splines stored as knot values in FP32) or K points
+(default 64) with batched shape `shape_index` (an entry of
+Engine.compiled_shapes(); -1 or none: the autotuner picks one first, and the
+chosen index is printed).
 
 train: the C2 surrogate network (200 -> 512 -> 512 -> 512 -> 3000, BF16)
 trained for `steps` (default 8) Adam steps of batch 2048 on a device-resident
@@ -67,13 +68,13 @@ def main(argv):
     precision = argv[1]
     n = int(argv[2]) if len(argv) > 2 else 1000000
     wl = Workload("c2", n_events=n, seed=2)
-    K = 64 if mode == "batched" else 1
-    eng = Engine.from_workload(wl, precision=precision, k_max=K)
+    K = (int(argv[4]) if len(argv) > 4 else 64) if mode == "batched" else 1
+    eng = Engine.from_workload(wl, precision=precision, k_max=max(K, 64) if mode == "batched" else 1)
     if mode == "batched":
-        if len(argv) > 3:
+        if len(argv) > 3 and int(argv[3]) >= 0:
             eng.set_shape_index(int(argv[3]))
         else:
-            eng.autotune(64)
+            eng.autotune(K)
     pts = wl.draw_points(K, 5)
     for _ in range(4):
         eng.eval(pts)

@@ -269,13 +269,14 @@ int gw_set_plain_kernel(gw_engine* e, int32_t kind);
 int gw_get_plain_kernel(const gw_engine* e, int32_t* kind);
 
 /* Copies the batched shape in use out: kernel family (0 = lanes over points,
- * 1 = threads over dials), parameter points per pass, threads per block,
- * payload stages. */
+ * 1 = threads over dials, 3 = warp-specialised threads over dials for small
+ * K), parameter points per pass, threads per block, payload stages. */
 int gw_get_shape(const gw_engine* e, int32_t* kind, int32_t* points_per_pass, int32_t* threads, int32_t* stages);
 
 /* The compiled batched shapes, for sweeps and tests.  gw_shape_count()
  * entries; gw_shape_at copies entry i out: family, points per pass, points
- * per thread, threads per block, payload stages and min_blocks (the CTAs per
+ * per thread (family 3: each evaluator thread takes all the points of a
+ * pass), threads per block, payload stages and min_blocks (the CTAs per
  * SM its launch bounds ask the compiler to fit; 0 = the compiler's choice).
  * A shape may be compiled for several register targets; gw_set_shape takes
  * the first.  Such variants give identical results.  gw_set_shape_index

@@ -161,7 +161,9 @@ def test_compiled_shape_list():
     shapes = Engine.compiled_shapes()
     assert len(shapes) >= 10
     for kind, ppp, ppt, threads, stages, minb in shapes:
-        assert kind in (0, 1) and threads in (128, 256) and stages in (1, 2) and minb >= 0
+        assert kind in (0, 1, 3) and threads in (128, 256) and stages in (1, 2) and minb >= 0
+        if kind == 3:  # small-K warp-specialised: every evaluator thread takes all points of a pass
+            assert ppp == ppt and ppp % 2 == 0 and threads == 256
         if kind == 0:
             assert ppp % ppt == 0 and ppp // ppt in (8, 16, 32)
     assert len(set(shapes)) == len(shapes)
