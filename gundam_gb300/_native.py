@@ -119,6 +119,7 @@ _D = C.c_double
 # name -> argtypes for every gw_* entry point declared in include/gw.h
 GW_SIGNATURES: dict[str, list] = {
     "gw_using_cuda": [_P],
+    "gw_llh_bins": [_I32, _P, _P, _P, _I32, _P],
     "gw_has_gpu": [_P],
     "gw_create": [_P, _P],
     "gw_destroy": [_P],

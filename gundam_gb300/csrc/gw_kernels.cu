@@ -604,6 +604,49 @@ cudaError_t launch_bins_llh(const DevView& v, int K, double* sums, double* sums2
 
 }  // namespace gw
 
+// ---------------------------------------------------------------------------
+// Per-bin likelihood terms on the device, one thread per bin: the same device
+// functions k_bins_llh sums.
+// ---------------------------------------------------------------------------
+namespace gw {
+namespace {
+__global__ void k_llh_bins(int type, const double* data, const double* pred, const double* sqrt_sum_w2, int n,
+                           double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = type == GW_LLH_POISSON ? llh_poisson(data[i], pred[i]) : llh_bb_bin(data[i], pred[i], sqrt_sum_w2[i]);
+}
+}  // namespace
+}  // namespace gw
+
+extern "C" int gw_llh_bins(int32_t llh_type, const double* data, const double* pred, const double* sqrt_sum_w2,
+                           int32_t n, double* out) {
+  if (!data || !pred || !sqrt_sum_w2 || !out || n < 0 ||
+      (llh_type != GW_LLH_POISSON && llh_type != GW_LLH_BARLOW_BEESTON_OA2021))
+    return GW_ERR_ARG;
+  if (n == 0) return GW_OK;
+  double* d = nullptr;
+  const size_t bytes = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&d, 4 * bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return GW_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMemcpy(d, data, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, pred, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 2 * (size_t)n, sqrt_sum_w2, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    gw::k_llh_bins<<<(n + 255) / 256, 256>>>(llh_type, d, d + n, d + 2 * (size_t)n, n, d + 3 * (size_t)n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return GW_ERR_CUDA;
+  }
+  return GW_OK;
+}
+
 // Compiled by the CUDA compiler: the device code above is in this library.
 extern "C" int gw_using_cuda(int32_t* using_cuda) {
   if (!using_cuda) return GW_ERR_ARG;

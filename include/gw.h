@@ -307,6 +307,17 @@ int gw_set_profiling(gw_engine* e, int32_t on);
  * kernel_launches counts every engine kernel launched.  Resets the sums. */
 int gw_read_profile(gw_engine* e, double* weights_ms, int64_t* weights_launches, int64_t* kernel_launches);
 
+/* Per-bin likelihood terms, each bin as JointProbabilityBase::eval(const
+ * SamplePair&, int) takes it (JointProbabilityBase.h:37-43 for
+ * GW_LLH_POISSON, PoissonLogLikelihood.h:19-53; BarlowBeestonBanff2022.h:92-294
+ * for GW_LLH_BARLOW_BEESTON_OA2021) from a histogram holding data[i], pred[i]
+ * (sum of weights) and sqrt_sum_w2[i] (sqrt of the sum of squared weights),
+ * evaluated on the device by the functions gw_eval's reduction sums.  Host
+ * arrays of n values; out[i] = the bin's term, +inf (or NaN) where the
+ * reference's default configuration throws (its throwIfInfLlh = false value). */
+int gw_llh_bins(int32_t llh_type, const double* data, const double* pred, const double* sqrt_sum_w2, int32_t n,
+                double* out);
+
 /* Likelihood from bin sums the caller holds on the device, with no device
  * allocation.  No counterpart in the reference.  For callers that cannot call
  * cudaMalloc: code running inside a framework that owns the GPU's memory (a

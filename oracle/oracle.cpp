@@ -343,6 +343,9 @@ double llh_bin(int type, double data, double pred, double sqrt_sum2) {
   if (type == 2) {
     double mcuncert = sqrt_sum2;  // BarlowBeestonBanff2022.h:126-127: sqrtSumSqWeights squared
     mcuncert *= mcuncert;
+    // BarlowBeestonBanff2022.h:130-144: a non-finite or negative value is +inf
+    // (throwIfInfLlh = false; the default configuration ends the process)
+    if (!std::isfinite(mcuncert) || mcuncert < 0.0) return std::numeric_limits<double>::infinity();
     return bb_oa2021(data, pred, mcuncert);
   }
   return 0.0;

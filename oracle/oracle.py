@@ -137,6 +137,39 @@ def ref_lib():
     return _ref
 
 
+REF_LLH = REF.parent / "libref_llh.so"
+_ref_llh = None
+
+
+def ref_llh_lib():
+    """GUNDAM's own per-bin likelihood classes compiled for the host (only
+    where oracle/_ref was built from the reference tree)."""
+    global _ref_llh
+    if _ref_llh is None and REF_LLH.exists():
+        lib_ = C.CDLL(str(REF_LLH))
+        lib_.ref_llh_bins.argtypes = [C.c_int32, _P, _P, _P, C.c_int32, _P, _P]
+        lib_.ref_llh_bins.restype = C.c_int
+        _ref_llh = lib_
+    return _ref_llh
+
+
+def ref_llh_bins(llh_type: int, data, pred, sqrt_sum_w2):
+    """(values, threw) of the reference's per-bin likelihood; None without _ref."""
+    lib_ = ref_llh_lib()
+    if lib_ is None:
+        return None
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    p = np.ascontiguousarray(pred, dtype=np.float64)
+    s = np.ascontiguousarray(sqrt_sum_w2, dtype=np.float64)
+    out = np.empty(d.size)
+    threw = np.zeros(d.size, dtype=np.int32)
+    rc = lib_.ref_llh_bins(llh_type, d.ctypes.data, p.ctypes.data, s.ctypes.data, d.size, out.ctypes.data,
+                           threw.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("ref_llh_bins failed")
+    return out, threw
+
+
 REF_CACHE = REF.parent / "libref_cache.so"
 _ref_cache = None
 

@@ -1,4 +1,4 @@
-"""Builds, from the reference's own sources where they lie, two host
+"""Builds, from the reference's own sources where they lie, three host
 libraries into oracle/_ref/ (never committed; test infrastructure):
 
 * libref_dials.so: the per-dial response functions (src/Utils/include/
@@ -7,7 +7,11 @@ libraries into oracle/_ref/ (never committed; test infrastructure):
   (src/CacheManager/src/{CacheParameters, CacheWeights, WeightBase,
   WeightNormalization, Weight*Spline, WeightGraph, WeightBilinear,
   CacheRecursiveSums, CacheAtomicCAS}.cpp with HEMI_CUDA_DISABLE and the
-  stand-in headers of oracle/ref/stubs/) behind oracle/ref/ref_cache.cpp.
+  stand-in headers of oracle/ref/stubs/) behind oracle/ref/ref_cache.cpp;
+* libref_llh.so: GUNDAM's per-bin likelihood classes (src/StatisticalInference/
+  JointProbability/include/{PoissonLogLikelihood, BarlowBeestonBanff2022}.h,
+  header-only, with the stand-ins of oracle/ref/stubs/) behind
+  oracle/ref/ref_llh.cpp.
 
 Usage: python oracle/ref/build_ref.py <path of the GUNDAM source tree>
 """
@@ -35,6 +39,10 @@ def main(reference: str) -> None:
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-DHEMI_CUDA_DISABLE",
            "-I", str(HERE / "stubs"), "-I", str(cm / "include"), "-I", str(inc),
            str(HERE / "ref_cache.cpp"), *srcs, "-o", str(OUT / "libref_cache.so")]
+    subprocess.run(cmd, check=True)
+    jp = Path(reference) / "src" / "StatisticalInference" / "JointProbability" / "include"
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+           "-I", str(HERE / "stubs"), "-I", str(jp), str(HERE / "ref_llh.cpp"), "-o", str(OUT / "libref_llh.so")]
     subprocess.run(cmd, check=True)
 
 

@@ -1,6 +1,7 @@
-// Minimal logger for compiling GUNDAM's Cache::Manager calculators on the host
-// outside the GUNDAM build (test infrastructure): informational output goes
-// nowhere, errors throw std::runtime_error with the streamed message.
+// Minimal logger for compiling GUNDAM's Cache::Manager calculators and its
+// likelihood classes on the host outside the GUNDAM build (test
+// infrastructure): informational output goes nowhere, errors throw
+// std::runtime_error with the streamed message.
 #ifndef GW_REF_STUB_LOGGER_H
 #define GW_REF_STUB_LOGGER_H
 #include <iostream>
@@ -21,6 +22,15 @@ inline NullStream& null_stream() {
 #define LogDebug gw_ref_stub::null_stream()
 #define LogWarning gw_ref_stub::null_stream()
 #define LogError gw_ref_stub::null_stream()
+#define LogAlert gw_ref_stub::null_stream()
+#define LogTrace gw_ref_stub::null_stream()
+#define LogErrorOnce gw_ref_stub::null_stream()
+#define LogErrorIf(cond_) gw_ref_stub::null_stream()
+#define LogTraceIf(cond_) gw_ref_stub::null_stream()
+#define LogScopeIndent \
+  do {                 \
+  } while (0)
+#define GET_VAR_NAME_VALUE(var_) #var_ << " = " << (var_)
 #define LogThrow(msg_)                   \
   do {                                   \
     std::ostringstream gw_ref_os_;       \
