@@ -45,9 +45,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true")
-    ap.add_argument("--mcmc-steps", type=int, default=6000)
-    ap.add_argument("--mcmc-train", type=int, default=131072)
-    ap.add_argument("--mcmc-epochs", type=int, default=100)
+    ap.add_argument("--no-c5", action="store_true")
+    ap.add_argument("--mcmc-steps", type=int, default=20000)
+    ap.add_argument("--mcmc-base-only-steps", type=int, default=4000)
+    ap.add_argument("--mcmc-train", type=int, default=1 << 20)
+    ap.add_argument("--mcmc-epochs", type=int, default=20)
     ap.add_argument("--mcmc-nsub", type=int, default=40)
     ap.add_argument("--mcmc-stage1", default="hmc", choices=["hmc", "rwm"])
     return ap.parse_args()
@@ -232,6 +234,57 @@ def time_device(eng, torch, d, K, steps, warmup, dist):
     return ms, kms / max(1, klaunch), launches
 
 
+def errors_vs_oracle(sums, llh, ref):
+    """Largest per-bin relative error of the bin sums (bins the oracle leaves
+    empty must be 0 exactly) and largest absolute LLH error."""
+    import numpy as np
+
+    r = ref["sums"]
+    occ = r != 0
+    rel = np.abs(sums[occ] - r[occ]) / np.abs(r[occ])
+    return {"max_bin_rel_err": float(rel.max(initial=0.0)),
+            "empty_bins_exact": bool(np.all(sums[~occ] == 0.0)),
+            "max_llh_abs_err": float(np.max(np.abs(llh - ref["llh"])))}
+
+
+def c1_points(local, n_points=1000):
+    """C1 (100k events, Poisson LLH, 20 parameters): bin contents and LLH at
+    1000 random parameter points from the prior, FP64 engine (the plain K = 1
+    kernel point by point, and all 1000 in batched launches of 250) and FP32
+    dials, each against the FP64 oracle on the same points; rates through
+    gw_eval with host buffers."""
+    from gundam_gb300 import Engine, Workload
+    from oracle.oracle import Oracle
+
+    wl = Workload("c1", seed=2)
+    pts = wl.draw_points(n_points, 2024)
+    t0 = time.perf_counter()
+    orc = Oracle(wl, llh_type=llh_type_for("c1"))
+    ref = orc.eval(pts)
+    orc.close()
+    out = {"workload": f"c1: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
+           "points": n_points, "oracle_seconds": time.perf_counter() - t0,
+           "tolerance": {"fp64": "per-bin relative 1e-12, LLH absolute 1e-6",
+                         "fp32": "per-bin relative 2e-5, LLH absolute 5e-2"}}
+    import numpy as np
+
+    for prec, K in (("fp64", 1), ("fp64", 250), ("fp32", 250)):
+        eng = Engine.from_workload(wl, precision=prec, k_max=K, llh_type=llh_type_for("c1"), device=local)
+        eng.autotune(K)
+        sums = np.empty((n_points, wl.n_bins))
+        llh = np.empty(n_points)
+        eng.eval(pts[:K])
+        t0 = time.perf_counter()
+        for a in range(0, n_points, K):
+            s_, _, l_, _ = eng.eval(pts[a:a + K])
+            sums[a:a + K], llh[a:a + K] = s_, l_
+        dt = time.perf_counter() - t0
+        out[f"{prec}_K{K}"] = dict(errors_vs_oracle(sums, llh, ref), evals_per_s=n_points / dt,
+                                   launches_of_points=K)
+        eng.close()
+    return out
+
+
 def c3_sweep(local, steps=20, warmup=3):
     """Batched reweighting of the 100k-event C1 workload: LLH evaluations/s at
     K = 16, 64, 256 points per launch (FP32 dials, FP64 sums and LLH, the
@@ -240,6 +293,7 @@ def c3_sweep(local, steps=20, warmup=3):
     import torch
 
     from gundam_gb300 import Engine, Workload
+    from oracle.oracle import Oracle
 
     wl = Workload("c1", seed=2)
     out = {"workload": f"c1: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
@@ -264,9 +318,14 @@ def c3_sweep(local, steps=20, warmup=3):
         b.record(stream)
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / steps
-        out[f"K{K}"] = {"evals_per_s": K * 1e3 / ms, "ms_per_launch": ms, "shape": list(eng.shape())}
+        sh, lh = s.cpu().numpy(), ll.cpu().numpy()
         eng.sync()
+        orc = Oracle(wl, llh_type=llh_type_for("c1"))
+        err = errors_vs_oracle(sh, lh, orc.eval(pts.cpu().numpy()))
+        orc.close()
+        out[f"K{K}"] = dict({"evals_per_s": K * 1e3 / ms, "ms_per_launch": ms, "shape": list(eng.shape())}, **err)
         eng.close()
+    out["error_against"] = "the FP64 oracle on the same K points (FP32 dials, FP64 sums and LLH)"
     return out
 
 
@@ -282,7 +341,8 @@ def mcmc_comparison(args):
 
     r = da_mcmc.run(events=args.events, train=args.mcmc_train, epochs=args.mcmc_epochs, steps=args.mcmc_steps,
                     n_sub=args.mcmc_nsub, seed=args.seed, config=args.config, precision=args.precision,
-                    linear=False, lr=2e-3, thin=2, stage1=args.mcmc_stage1)
+                    linear=True, base_only_steps=args.mcmc_base_only_steps, lr=2e-3, thin=2,
+                    stage1=args.mcmc_stage1)
     p, d = r["plain"], r["delayed"]
     return {
         "metric": "ESS/s, surrogate delayed acceptance vs plain engine MCMC (same GPU)",
@@ -300,6 +360,23 @@ def mcmc_comparison(args):
                      "loss_first_last": r["training"]["loss_first_last"]},
         "ess": "multi-chain (Vehtari et al. 2021) with Geyer's initial monotone sequence; chains of this length "
                "underestimate the plain sampler's autocorrelation time, so the gain here is a lower estimate",
+        "network_gain": {"base_only_ess_per_s_median": r.get("delayed_base_only", {}).get("ess_per_s_median"),
+                         "base_only_steps": args.mcmc_base_only_steps,
+                         "delayed_over_base_only_median": r.get("network_gain_ess_per_s_median")},
+        "config_departures": {
+            "steps_each": f"{r['plain_steps']} (stated: 100000; the full-length run is recorded in "
+                          "profiles/c4_da_mcmc_full.md)" if r["plain_steps"] != 100000 else None,
+            "training_points": None if r["training"]["points"] == 1 << 20 else r["training"]["points"],
+            "epochs": None if r["training"]["epochs"] == 20 else r["training"]["epochs"],
+            "proposal": "the adaptive pilot's covariance and scale (GUNDAM's SimpleMcmc adaptive proposal), not "
+                        "2.38^2/200 x the prior covariance: at 5M events the posterior is ~5x narrower than "
+                        "the prior and that proposal accepts ~0.6 %",
+            "training_region": "the pilot's posterior mean and covariance inflated x1.5, not the prior inflated "
+                               "x1.5: a surrogate trained on prior draws errs by ~800 in -2 log L at posterior "
+                               "states",
+            "stage1": "Hamiltonian Monte Carlo on the surrogate (10 leapfrog steps) instead of one random-walk "
+                      "step per stage-2 correction" if r["stage1"]["kind"] == "hmc" else None,
+        },
     }
 
 
@@ -389,6 +466,25 @@ def run_gw(args, world, rank, local, dist):
             "kernel_frac_of_hbm_peak": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9 / peak,
             "payload_bytes": e1.layout()["payload_bytes"], "spline_layout": "knots"}
         e1.close()
+        for Ks in (2, 4):
+            # small K: the warp-specialised small-K kernels, autotuned; e2e
+            # through gw_eval with host buffers
+            eng.autotune(Ks)
+            msk, kmsk, _ = time_device(eng, torch, d, Ks, args.steps, args.warmup, dist)
+            pk = pts[:Ks]
+            for _ in range(2):
+                eng.eval(pk)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                eng.eval(pk)
+            e2e_k = (time.perf_counter() - t0) / args.steps
+            algk = algorithmic_bytes(wl, args.precision, Ks)
+            sk = eng.shape_index()
+            variants[f"{args.precision}_K{Ks}"] = {
+                "shape": list(Engine.compiled_shapes()[sk]), "evals_per_s": Ks * 1e3 / msk, "ms_per_step": msk,
+                "kernel_ms": kmsk, "kernel_gbs": algk / (kmsk / 1e3) / 1e9,
+                "kernel_frac_of_hbm_peak": algk / (kmsk / 1e3) / 1e9 / peak,
+                "e2e_evals_per_s": Ks / e2e_k, "e2e_ms_per_step": e2e_k * 1e3}
         if K > 16:
             # C3 at the C2 size: K = 16 on this engine, K = 256 on one sized for it
             eng.autotune(16)
@@ -433,9 +529,18 @@ def run_gw(args, world, rank, local, dist):
         # scales with cores; the single-core rate shows the per-core cost)
         v1, _, n1, dt1 = cpu_baseline(wl, args.config, max(1.0, args.cpu_seconds / 4), threads=1)
         cpu["one_core"] = {"value": v1, "sample": f"{n1} full evaluations on 1 thread, {dt1:.1f} s"}
-    c3 = None
+    if cpu:
+        for key, var in variants.items():
+            if "e2e_evals_per_s" in var:
+                var["e2e_over_cpu_baseline"] = var["e2e_evals_per_s"] / cpu["value"]
+    c3 = c1 = c5 = None
     if rank == 0 and not args.no_variants:
         c3 = c3_sweep(local)
+        c1 = c1_points(local)
+    if rank == 0 and not args.no_c5 and args.config == "c2":
+        from gundam_gb300 import stress
+
+        c5 = stress.run()
     mc = None
     if rank == 0 and not args.no_mcmc and args.config == "c2":
         mc = mcmc_comparison(args)
@@ -467,6 +572,8 @@ def run_gw(args, world, rank, local, dist):
             "variants": variants,
             "event_dials_per_s": value * wl.n_dials,
             "c3_batched_vs_k": c3,
+            "c1_thousand_points": c1,
+            "c5_stress": c5,
             "mcmc": mc,
         }
         print(json.dumps(line), flush=True)

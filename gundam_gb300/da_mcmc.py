@@ -65,9 +65,11 @@ def _sampler_stats(ch, seconds, burn):
 def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=2, config="c2", log=None,
         precision="fp32", region="posterior", proposal="adapted", base_points=32768, nodes=8, batch=2048,
         lr=1e-3, linear=True, max_error=20.0, adapt_cycles=6, adapt_steps=200, da_steps=None, thin=1,
-        warm_steps=500, burn_frac=0.1, stage1="hmc", eps=0.25, n_leap=10):
+        warm_steps=500, burn_frac=0.1, stage1="hmc", eps=0.25, n_leap=10, base_only_steps=None):
     """Fit, adapt, train, then sample with both samplers from the same states
-    (``steps`` plain steps and ``da_steps`` (default: the same) delayed steps)."""
+    (``steps`` plain steps and ``da_steps`` (default: the same) delayed steps;
+    the base-only delayed arm, which shows what the network adds, runs
+    ``base_only_steps`` (default: ``da_steps``))."""
     log = log or (lambda *_: None)
     t_all = time.perf_counter()
     da_steps = da_steps or steps
@@ -213,8 +215,8 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
     p = mcmc.plain(f_exact, th0, steps, L, seed=seed + 7, thin=thin)
     d = mcmc.delayed(f_exact, f_sur, th0, da_steps, L, n_sub=n_sub, seed=seed + 8, stage1=stage1_of(sur),
                      thin=thin, **frozen)
-    dl = mcmc.delayed(f_exact, None, th0, da_steps, L, n_sub=n_sub, seed=seed + 9, max_error=float("inf"),
-                      stage1=stage1_of(lin), thin=thin) if lin else None
+    dl = mcmc.delayed(f_exact, None, th0, base_only_steps or da_steps, L, n_sub=n_sub, seed=seed + 9,
+                      max_error=float("inf"), stage1=stage1_of(lin), thin=thin) if lin else None
     bp = int(burn_frac * p["chains"].shape[0])
     bd = int(burn_frac * d["chains"].shape[0])
     ess_p, st_p = _sampler_stats(p["chains"], p["seconds"], bp)
@@ -263,8 +265,8 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
         "ess_per_s_gain_median": st_d["ess_per_s_median"] / st_p["ess_per_s_median"],
     }
     if dl is not None:
-        _, st_l = _sampler_stats(dl["chains"], dl["seconds"], bd)
-        res["delayed_base_only"] = dict(st_l, stage2_accept=dl["stage2_accept"],
+        _, st_l = _sampler_stats(dl["chains"], dl["seconds"], int(burn_frac * dl["chains"].shape[0]))
+        res["delayed_base_only"] = dict(st_l, steps=base_only_steps or da_steps, stage2_accept=dl["stage2_accept"],
                                         fell_back_at_step=dl["fell_back_at_step"],
                                         stage2_llh_error_mean=dl["surrogate_error_mean"])
         res["network_gain_ess_per_s_median"] = st_d["ess_per_s_median"] / st_l["ess_per_s_median"]

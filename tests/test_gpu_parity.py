@@ -76,8 +76,20 @@ def test_c1_fp32_plain(c1, c1_oracle):
     eng.close()
 
 
+def test_c1_thousand_points_fp64(c1, c1_oracle):
+    """C1's stated result: Poisson LLH and bin contents at 1000 random
+    parameter points, FP64, in four batched launches of 250 points."""
+    eng = Engine.from_workload(c1, precision="fp64", k_max=250, llh_type=N.GW_LLH_POISSON)
+    pts = c1.draw_points(1000, 1000)
+    ref = c1_oracle.eval(pts)
+    parts = [eng.eval(pts[a:a + 250]) for a in range(0, 1000, 250)]
+    out = tuple(np.concatenate([p[i] for p in parts]) for i in range(4))
+    _check(out, ref, FP64_BIN_REL, FP64_LLH_ABS, "1000 points")
+    eng.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("K", [2, 16, 64, 200])
+@pytest.mark.parametrize("K", [2, 4, 16, 64, 200, 256])
 def test_c1_batched(c1, c1_oracle, precision, K):
     eng = Engine.from_workload(c1, precision=precision, k_max=256, llh_type=N.GW_LLH_POISSON)
     pts = c1.draw_points(K, 100 + K)
