@@ -34,6 +34,7 @@ GW_DIAL_KRIGED = 10
 
 GW_FP64 = 0
 GW_FP32 = 1
+GW_DF64 = 2
 GW_FLAG_SPLINE_KNOTS = 1
 GW_FLAG_SPLINE_SLOPES = 2
 

@@ -15,6 +15,10 @@ namespace {
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { using type = double2; };
 template <> struct Vec2<float> { using type = float2; };
+struct __align__(16) dfloat2 {
+  dfloat x, y;
+};
+template <> struct Vec2<dfloat> { using type = dfloat2; };
 
 // ---------------------------------------------------------------------------
 // Bulk-copy (TMA) and mbarrier helpers.
@@ -130,7 +134,15 @@ __device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, 
 template <typename T, int KR, bool VX>
 __device__ __forceinline__ void load_points(const T* __restrict__ p, int kstep, T (&x)[KR]) {
   if constexpr (VX && (KR * sizeof(T)) % 16 == 0) {
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (kIsDf<T>) {
+      const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+      for (int i = 0; i < KR / 2; ++i) {
+        const float4 f = q[i];
+        x[2 * i] = dfloat(f.x, f.y);
+        x[2 * i + 1] = dfloat(f.z, f.w);
+      }
+    } else if constexpr (sizeof(T) == 4) {
       const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
       for (int i = 0; i < KR / 4; ++i) {

@@ -2,12 +2,16 @@
 //
 // Each function restates the arithmetic of the reference's shared CPU/GPU
 // headers in src/Utils/include/Calculate*.h, in the same operation order, for
-// T = double (FP64 mode) or T = float (FP32 mode).  Data is read from the tile
+// T = double (FP64 mode), T = float (FP32 mode) or T = dfloat (double-float
+// mode: the same operations in double-float arithmetic on the FP32 pipe).  Data is read from the tile
 // payload in shared memory.  The CPU dial wrappers call these with bounds
 // (-1e20, 1e20) and apply the collection's response clamp afterwards
 // (MonotonicSpline.cpp:71-84, DialResponseSupervisor.cpp:10-18); the engine
 // applies both as one clamp after the call (gw_kernels.cu, dial_values).
 #pragma once
+#include <type_traits>
+
+#include "gw_dfloat.h"
 #include "gw_layout.h"
 
 namespace gw {
@@ -16,6 +20,10 @@ namespace gw {
 // reciprocal-multiply form in FP32 mode (within the FP32 tolerance).
 __device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ dfloat fdiv(dfloat a, dfloat b) { return df_div(a, b); }
+
+template <typename T>
+constexpr bool kIsDf = std::is_same<T, dfloat>::value;
 
 // Hermite cubic on [p1, p2] with end slopes m1, m2 (already scaled by the
 // interval width), Horner form of CalculateUniformSpline.h:71-74.
@@ -131,6 +139,7 @@ __device__ __forceinline__ T eval_prepared(const T* __restrict__ d, int n, T x, 
 
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ dfloat mul_rn(dfloat a, dfloat b) { return a * b; }
 
 // Catmull-Rom knot slope from the differences on either side, with the
 // Fritsch-Carlson limiter when `limit` (CalculateMonotonicSpline.h:66-127);

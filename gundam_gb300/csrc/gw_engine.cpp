@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "gw.h"
+#include "gw_dfloat.h"
 #include "gw_internal.h"
 
 using namespace gw;
@@ -222,7 +223,7 @@ extern "C" int gw_create(const gw_config* c, gw_engine** out) {
   if (!c || !out) return fail(nullptr, GW_ERR_ARG, "null argument");
   *out = nullptr;
   if (c->n_results < 0 || c->n_params < 1 || c->n_params > 8192 || c->n_bins < 1 || c->k_max < 1 ||
-      c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32) ||
+      c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32 && c->precision != GW_DF64) ||
       (c->flags != 0 && c->flags != GW_FLAG_SPLINE_KNOTS && c->flags != GW_FLAG_SPLINE_SLOPES))
     return fail(nullptr, GW_ERR_ARG,
                 "bad gw_config (n_results=%d n_params=%d n_bins=%d k_max=%d precision=%d flags=%d)",
@@ -1153,8 +1154,12 @@ int build_and_upload(gw_engine* e) {
   if (bps < 1) return fail(e, GW_ERR_CUDA, "plain kernel does not fit on an SM");
   e->plain_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bps * e->num_sms));
   const int K0 = e->cfg.k_max;
-  if (K0 >= 8) e->shape = BatchedShape{1, 8, 4, 256, 1, 0};
-  else e->shape = BatchedShape{1, 4, 2, 256, 2, 0};
+  if (e->cfg.precision == GW_DF64)  // compiled for a subset of the shapes (gw_lanes.cu, gw_ws.cu)
+    e->shape = K0 >= 8 ? BatchedShape{0, 32, 1, 256, 1, 0} : BatchedShape{3, 2, 2, 256, 2, 2};
+  else if (K0 >= 8)
+    e->shape = BatchedShape{1, 8, 4, 256, 1, 0};
+  else
+    e->shape = BatchedShape{1, 4, 2, 256, 2, 0};
   const int bb = batched_blocks_per_sm(v, e->shape);
   if (bb < 1) return fail(e, GW_ERR_CUDA, "batched kernel does not fit on an SM");
   e->batched_grid = (int)std::max<int64_t>(1, std::min<int64_t>(T_, (int64_t)bb * e->num_sms));
@@ -1168,7 +1173,9 @@ extern "C" int gw_initialize(gw_engine* e) {
   GW_REQUIRE_BUILDER(e);
   int rc;
   try {
-    rc = e->cfg.precision == GW_FP32 ? build_and_upload<float>(e) : build_and_upload<double>(e);
+    rc = e->cfg.precision == GW_FP32   ? build_and_upload<float>(e)
+         : e->cfg.precision == GW_DF64 ? build_and_upload<dfloat>(e)
+                                       : build_and_upload<double>(e);
   } catch (const std::bad_alloc&) {
     rc = fail(e, GW_ERR_NOMEM, "host allocation failed while packing");
   }
@@ -1196,9 +1203,14 @@ static int refresh_tables(gw_engine* e) {
         if (rc) return rc;
       }
       unsigned char* dst = (unsigned char*)e->view.table_arena + off * tsz;
-      if (tsz == 8) {
+      if (e->cfg.precision == GW_FP64) {
         GW_CUDA(e, cudaMemcpyAsync(dst, h.values.data(), sizeof(double) * h.size, cudaMemcpyHostToDevice,
                                    e->stream));
+      } else if (e->cfg.precision == GW_DF64) {
+        std::vector<dfloat> f(h.size);
+        for (int64_t i = 0; i < (int64_t)h.size; ++i) f[i] = dfloat(h.values[i]);
+        GW_CUDA(e, cudaMemcpyAsync(dst, f.data(), sizeof(dfloat) * h.size, cudaMemcpyHostToDevice, e->stream));
+        GW_CUDA(e, cudaStreamSynchronize(e->stream));
       } else {
         std::vector<float> f(h.values.begin(), h.values.end());
         GW_CUDA(e, cudaMemcpyAsync(dst, f.data(), sizeof(float) * h.size, cudaMemcpyHostToDevice, e->stream));

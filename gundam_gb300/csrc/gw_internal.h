@@ -15,7 +15,7 @@ enum : uint32_t {
 
 // Every device pointer and size a launch needs.  Plain data, passed by value.
 struct DevView {
-  int precision;        // 0 = FP64, 1 = FP32
+  int precision;        // 0 = FP64, 1 = FP32, 2 = double-float (GW_DF64)
   int plain_kind;       // K = 1 kernel: 0 = k_plain, 1 = k_plain_ws (warp-specialised)
   int n_params;
   int n_bins;
@@ -87,11 +87,12 @@ int batched_shape_count();
 BatchedShape batched_shape(int i);
 
 // One compiled batched kernel: its function (for occupancy queries) and its
-// launcher, per precision [FP64, FP32].
+// launcher, per precision [FP64, FP32, double-float] (indexed by the
+// engine's precision value).
 struct ShapeEntry {
   int kind, kc, kr, threads, stages, minb;
-  const void* fn[2];
-  void (*launch[2])(const DevView&, int, int, size_t, cudaStream_t);
+  const void* fn[3];
+  void (*launch[3])(const DevView&, int, int, size_t, cudaStream_t);
 };
 int lane_shapes(const ShapeEntry** out);   // gw_lanes.cu
 int multi_shapes(const ShapeEntry** out);  // gw_multi.cu

@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
 // Launchers.
 // ---------------------------------------------------------------------------
 size_t plain_smem_bytes(const DevView& v) {
-  const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  const size_t tsz = v.precision == 1 ? sizeof(float) : sizeof(double);
   const size_t dv = (v.plain_kind == 1 ? 2048 : 1024) * tsz;
   const size_t hb = v.plain_kind == 1 ? 2 * (size_t)v.tile_hdr_bytes : 0;
   return 2 * (size_t)v.tile_payload_bytes + hb + dv + kMaxTileEvents * sizeof(double) +
@@ -455,7 +455,7 @@ size_t plain_smem_bytes(const DevView& v) {
 }
 
 size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
-  const size_t tsz = v.precision ? sizeof(float) : sizeof(double);
+  const size_t tsz = v.precision == 1 ? sizeof(float) : sizeof(double);
   if (b.kind == 3) return ws_smem_bytes(v, b.kc);  // k_ws
   if (b.kind == 1) {  // k_multi
     return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
@@ -510,6 +510,7 @@ static const ShapeEntry* find_shape(const BatchedShape& b) {
 }
 
 static const void* pick_plain(const DevView& v) {
+  if (v.precision == 2) return plain_fn<dfloat>(v.plain_kind);
   return v.precision ? plain_fn<float>(v.plain_kind) : plain_fn<double>(v.plain_kind);
 }
 
@@ -526,7 +527,8 @@ int plain_blocks_per_sm(const DevView& v) {
 int batched_blocks_per_sm(const DevView& v, const BatchedShape& b) {
   const ShapeEntry* e = find_shape(b);
   if (!e) return 0;
-  const void* fn = e->fn[v.precision ? 1 : 0];
+  const void* fn = e->fn[v.precision];
+  if (!fn) return 0;  // not compiled for this precision
   const size_t smem = batched_smem_bytes(v, b);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
@@ -544,13 +546,16 @@ size_t params_smem_bytes(const DevView& v) { return (size_t)v.n_params * sizeof(
 
 cudaError_t prepare_params(const DevView& v) {
   const size_t smem = params_smem_bytes(v);
-  const void* fn = v.precision ? (const void*)k_params<float> : (const void*)k_params<double>;
+  const void* fn = v.precision == 2 ? (const void*)k_params<dfloat>
+                    : v.precision ? (const void*)k_params<float> : (const void*)k_params<double>;
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStream_t s) {
   const size_t smem = params_smem_bytes(v);
-  if (v.precision)
+  if (v.precision == 2)
+    k_params<dfloat><<<K, 256, smem, s>>>(v, params);
+  else if (v.precision)
     k_params<float><<<K, 256, smem, s>>>(v, params);
   else
     k_params<double><<<K, 256, smem, s>>>(v, params);
@@ -560,7 +565,9 @@ cudaError_t launch_params(const DevView& v, const double* params, int K, cudaStr
 cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t s) {
   if (v.n_table_fns == 0) return cudaSuccess;
   dim3 grid((max_size + 255) / 256, v.n_table_fns);
-  if (v.precision)
+  if (v.precision == 2)
+    k_table_fn<dfloat><<<grid, 256, 0, s>>>(v, K);
+  else if (v.precision)
     k_table_fn<float><<<grid, 256, 0, s>>>(v, K);
   else
     k_table_fn<double><<<grid, 256, 0, s>>>(v, K);
@@ -570,12 +577,16 @@ cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
   const size_t smem = plain_smem_bytes(v);
   if (v.plain_kind == 1) {
-    if (v.precision)
+    if (v.precision == 2)
+      k_plain_ws<dfloat><<<grid, kPlainThreads, smem, s>>>(v);
+    else if (v.precision)
       k_plain_ws<float><<<grid, kPlainThreads, smem, s>>>(v);
     else
       k_plain_ws<double><<<grid, kPlainThreads, smem, s>>>(v);
   } else {
-    if (v.precision)
+    if (v.precision == 2)
+      k_plain<dfloat><<<grid, kPlainThreads, smem, s>>>(v);
+    else if (v.precision)
       k_plain<float><<<grid, kPlainThreads, smem, s>>>(v);
     else
       k_plain<double><<<grid, kPlainThreads, smem, s>>>(v);
@@ -590,8 +601,8 @@ bool batched_shape_covers(const DevView& v, const BatchedShape& b, int K) {
 
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s) {
   const ShapeEntry* e = find_shape(b);
-  if (!e || !batched_shape_covers(v, b, K)) return cudaErrorInvalidValue;
-  e->launch[v.precision ? 1 : 0](v, K, grid, batched_smem_bytes(v, b), s);
+  if (!e || !e->launch[v.precision] || !batched_shape_covers(v, b, K)) return cudaErrorInvalidValue;
+  e->launch[v.precision](v, K, grid, batched_smem_bytes(v, b), s);
   return cudaGetLastError();
 }
 

@@ -179,20 +179,31 @@ void launch_b(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
   k_batched<T, KC, KR, NT, ST, MB><<<grid, NT, smem, s>>>(v, K);
 }
 
-#define GW_SHAPE(KC, KR, NT, ST, MB)                                                           \
-  {0, KC, KR, NT, ST, MB, {(const void*)k_batched<double, KC, KR, NT, ST, MB>,                \
-                           (const void*)k_batched<float, KC, KR, NT, ST, MB>},                 \
-   {launch_b<double, KC, KR, NT, ST, MB>, launch_b<float, KC, KR, NT, ST, MB>}}
+// GW_SHAPE compiles the shape for FP64, FP32 and double-float; GW_SHAPE2 for
+// FP64 and FP32 only (double-float needs more registers than the 3- and
+// 4-CTA-per-SM targets give it, and each instantiation costs build time).
+#define GW_SHAPE(KC, KR, NT, ST, MB)                                                                   \
+  {0, KC, KR, NT, ST, MB,                                                                              \
+   {(const void*)k_batched<double, KC, KR, NT, ST, MB>, (const void*)k_batched<float, KC, KR, NT, ST, MB>, \
+    (const void*)k_batched<dfloat, KC, KR, NT, ST, MB>},                                               \
+   {launch_b<double, KC, KR, NT, ST, MB>, launch_b<float, KC, KR, NT, ST, MB>,                         \
+    launch_b<dfloat, KC, KR, NT, ST, MB>}}
+#define GW_SHAPE2(KC, KR, NT, ST, MB)                                                                  \
+  {0, KC, KR, NT, ST, MB,                                                                              \
+   {(const void*)k_batched<double, KC, KR, NT, ST, MB>, (const void*)k_batched<float, KC, KR, NT, ST, MB>, \
+    nullptr},                                                                                          \
+   {launch_b<double, KC, KR, NT, ST, MB>, launch_b<float, KC, KR, NT, ST, MB>, nullptr}}
 
 // (32, 2, 256, 1) with 3 and 4 CTAs per SM are the fastest at K = 64 on the
 // 5M-event mixed workload (9.5 / 9.4 ms against 11.2 ms with the compiler's
 // own register choice); the others cover small K and K >= 128.
 const ShapeEntry kLaneShapes[] = {
-    GW_SHAPE(8, 1, 256, 2, 0),  GW_SHAPE(16, 1, 256, 2, 0), GW_SHAPE(32, 1, 256, 2, 0),
-    GW_SHAPE(32, 1, 256, 1, 0), GW_SHAPE(32, 2, 256, 1, 3), GW_SHAPE(32, 2, 256, 1, 4),
-    GW_SHAPE(32, 2, 256, 2, 3), GW_SHAPE(32, 2, 128, 1, 6), GW_SHAPE(32, 4, 128, 1, 0),
-    GW_SHAPE(16, 2, 256, 1, 0), GW_SHAPE(32, 4, 256, 1, 2),
+    GW_SHAPE2(8, 1, 256, 2, 0), GW_SHAPE(16, 1, 256, 2, 0),  GW_SHAPE2(32, 1, 256, 2, 0),
+    GW_SHAPE(32, 1, 256, 1, 0), GW_SHAPE2(32, 2, 256, 1, 3), GW_SHAPE2(32, 2, 256, 1, 4),
+    GW_SHAPE2(32, 2, 256, 2, 3), GW_SHAPE2(32, 2, 128, 1, 6), GW_SHAPE2(32, 4, 128, 1, 0),
+    GW_SHAPE(16, 2, 256, 1, 0),  GW_SHAPE2(32, 4, 256, 1, 2),
 };
+#undef GW_SHAPE2
 #undef GW_SHAPE
 
 }  // namespace

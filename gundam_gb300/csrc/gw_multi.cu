@@ -130,10 +130,12 @@ void launch_m(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
   k_multi<T, KCH, KR, ST><<<grid, 256, smem, s>>>(v, K);
 }
 
+// FP64 and FP32 only: in double-float the small-K warp-specialised kernels
+// (gw_ws.cu) take this family's range of K.
 #define GW_MULTI(KCH, KR, ST)                                                                  \
-  {1, KCH, KR, 256, ST, 0, {(const void*)k_multi<double, KCH, KR, ST>,                         \
-                         (const void*)k_multi<float, KCH, KR, ST>},                             \
-   {launch_m<double, KCH, KR, ST>, launch_m<float, KCH, KR, ST>}}
+  {1, KCH, KR, 256, ST, 0,                                                                     \
+   {(const void*)k_multi<double, KCH, KR, ST>, (const void*)k_multi<float, KCH, KR, ST>, nullptr}, \
+   {launch_m<double, KCH, KR, ST>, launch_m<float, KCH, KR, ST>, nullptr}}
 
 const ShapeEntry kMultiShapes[] = {
     GW_MULTI(2, 2, 2), GW_MULTI(4, 2, 2), GW_MULTI(4, 4, 1), GW_MULTI(4, 4, 2),

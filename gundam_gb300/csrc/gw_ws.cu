@@ -32,7 +32,11 @@ constexpr int kSBarEval = 1, kSBarFull = 2, kSBarEmpty = 4, kSBarRed = 6;
 // The KP values of one slot: stores, loads and the elementwise product.
 template <typename T, int KP>
 __device__ __forceinline__ void slot_store(T* dst, const T (&v)[KP]) {
-  if constexpr (sizeof(T) == 4 && KP == 2) {
+  if constexpr (kIsDf<T>) {
+#pragma unroll
+    for (int j = 0; j < KP; j += 2)
+      *(float4*)(dst + j) = make_float4(v[j].hi, v[j].lo, v[j + 1].hi, v[j + 1].lo);
+  } else if constexpr (sizeof(T) == 4 && KP == 2) {
     *(float2*)dst = make_float2(v[0], v[1]);
   } else if constexpr (sizeof(T) == 4 && KP % 4 == 0) {
 #pragma unroll
@@ -45,7 +49,14 @@ __device__ __forceinline__ void slot_store(T* dst, const T (&v)[KP]) {
 
 template <typename T, int KP>
 __device__ __forceinline__ void slot_mul(T (&w)[KP], const T* src) {
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (kIsDf<T>) {
+#pragma unroll
+    for (int j = 0; j < KP; j += 2) {
+      const float4 a = *(const float4*)(src + j);
+      w[j] *= dfloat(a.x, a.y);
+      w[j + 1] *= dfloat(a.z, a.w);
+    }
+  } else if constexpr (sizeof(T) == 4) {
 #pragma unroll
     for (int j = 0; j < KP; j += 2) {
       const float2 a = *(const float2*)(src + j);
@@ -234,14 +245,20 @@ void launch_s(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
 }
 
 // kind 3: points per pass KP (= points per evaluator thread), 256 threads, 2 stages
-#define GW_WS(KP, MB)                                                                                  \
-  {3, KP, KP, kSThreads, 2, MB, {(const void*)k_ws<double, KP, MB>, (const void*)k_ws<float, KP, MB>}, \
-   {launch_s<double, KP, MB>, launch_s<float, KP, MB>}}
+// GW_WS: FP64, FP32 and double-float; GW_WS2: FP64 and FP32 only.
+#define GW_WS(KP, MB)                                                                                 \
+  {3, KP, KP, kSThreads, 2, MB,                                                                       \
+   {(const void*)k_ws<double, KP, MB>, (const void*)k_ws<float, KP, MB>, (const void*)k_ws<dfloat, KP, MB>}, \
+   {launch_s<double, KP, MB>, launch_s<float, KP, MB>, launch_s<dfloat, KP, MB>}}
+#define GW_WS2(KP, MB)                                                                                \
+  {3, KP, KP, kSThreads, 2, MB, {(const void*)k_ws<double, KP, MB>, (const void*)k_ws<float, KP, MB>, nullptr}, \
+   {launch_s<double, KP, MB>, launch_s<float, KP, MB>, nullptr}}
 
 const ShapeEntry kWsShapes[] = {
-    GW_WS(2, 3), GW_WS(2, 2), GW_WS(4, 3), GW_WS(4, 2), GW_WS(8, 2),
+    GW_WS2(2, 3), GW_WS(2, 2), GW_WS2(4, 3), GW_WS(4, 2), GW_WS2(8, 2),
 };
 #undef GW_WS
+#undef GW_WS2
 
 }  // namespace
 
@@ -251,7 +268,7 @@ int ws_shapes(const ShapeEntry** out) {
 }
 
 size_t ws_smem_bytes(const DevView& v, int kc) {
-  const bool f = v.precision != 0;
+  const bool f = v.precision == 1;  // FP32; FP64 and double-float values are 8 bytes
   switch (kc) {
     case 2: return f ? ws_bytes<float, 2>(v) : ws_bytes<double, 2>(v);
     case 4: return f ? ws_bytes<float, 4>(v) : ws_bytes<double, 4>(v);

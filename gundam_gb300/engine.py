@@ -30,8 +30,9 @@ class Engine:
         the host) or "auto" (knots for an FP32 engine with k_max == 1)."""
         self.lib = N.libgw()
         flags = {"auto": 0, "knots": N.GW_FLAG_SPLINE_KNOTS, "slopes": N.GW_FLAG_SPLINE_SLOPES}[spline_layout]
-        cfg = N.GwConfig(int(n_results), int(n_params), int(n_bins), int(k_max),
-                         N.GW_FP32 if precision == "fp32" else N.GW_FP64, int(device), int(tile_bytes), flags)
+        prec = {"fp32": N.GW_FP32, "fp64": N.GW_FP64, "df64": N.GW_DF64}[precision]
+        cfg = N.GwConfig(int(n_results), int(n_params), int(n_bins), int(k_max), prec, int(device), int(tile_bytes),
+                         flags)
         p = C.c_void_p()
         N.check(self.lib.gw_create(C.byref(cfg), C.byref(p)), None)
         self._e = p

@@ -64,7 +64,9 @@ enum {
 /* ---- precision of dial math and of the per-event weight product -------- */
 enum {
   GW_FP64 = 0, /* everything in FP64, as the reference (WeightBase.h:19) */
-  GW_FP32 = 1  /* dials + weight product in FP32; bin sums, sum of w^2, LLH in FP64 */
+  GW_FP32 = 1, /* dials + weight product in FP32; bin sums, sum of w^2, LLH in FP64 */
+  GW_DF64 = 2  /* dials + weight product in double-float (two FP32 words per value, ~48
+                  significant bits, on the FP32 pipe); bin sums, sum of w^2, LLH in FP64 */
 };
 
 /* ---- gw_config.flags: stored form of Catmull-Rom (monotonic, compact)
@@ -106,7 +108,7 @@ typedef struct gw_config {
   int32_t n_params;   /* parameters in the cache (<= 65535) */
   int32_t n_bins;     /* global histogram cells */
   int32_t k_max;      /* largest number of parameter points per gw_eval (>= 1) */
-  int32_t precision;  /* GW_FP64 or GW_FP32 */
+  int32_t precision;  /* GW_FP64, GW_FP32 or GW_DF64 */
   int32_t device;     /* CUDA device ordinal */
   int32_t tile_bytes; /* payload bytes per tile; 0 = default (28672 FP32, 32768 FP64) */
   int32_t flags;      /* 0 or one GW_FLAG_SPLINE_* value */

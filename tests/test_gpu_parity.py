@@ -5,6 +5,10 @@ Tolerances (FP64 mode, as the acceptance bar states): per-bin relative error
 absolute error <= 1e-6.  FP32 mode (dial math and weight product in FP32,
 bins / sum of w^2 / likelihood in FP64): per-bin relative error <= 2e-5 and
 likelihood absolute error <= 5e-2 (stated in FP32_* below).
+
+Double-float mode (precision "df64": dial arithmetic and the weight product
+in two-FP32-word numbers on the FP32 pipe, sums and likelihood in FP64) is
+held to the FP64 bar above; its per-event weights to 1e-12 relative.
 """
 import json
 from pathlib import Path
@@ -22,6 +26,14 @@ FP64_BIN_REL = 1e-12
 FP64_LLH_ABS = 1e-6
 FP32_BIN_REL = 2e-5
 FP32_LLH_ABS = 5e-2
+# double-float mode (GW_DF64: dials and weight products in two-FP32-word
+# arithmetic, ~48 significant bits; sums and likelihood in FP64) is held to
+# the FP64 bar; its per-event weights carry a few 2^-48 of rounding
+DF64_EVENT_REL = 1e-12
+
+
+def _tol(precision):
+    return (FP32_BIN_REL, FP32_LLH_ABS) if precision == "fp32" else (FP64_BIN_REL, FP64_LLH_ABS)
 
 
 def _bin_rel(got, ref):
@@ -60,8 +72,9 @@ def mixed_oracle(mixed):
     return Oracle(mixed, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
 
 
-def test_c1_fp64_plain(c1, c1_oracle):
-    eng = Engine.from_workload(c1, precision="fp64", k_max=1, llh_type=N.GW_LLH_POISSON)
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_c1_plain(c1, c1_oracle, precision):
+    eng = Engine.from_workload(c1, precision=precision, k_max=1, llh_type=N.GW_LLH_POISSON)
     pts = np.vstack([c1.nominal(), c1.draw_points(24, 5)])
     for i, p in enumerate(pts):
         _check(eng.eval(p[None]), c1_oracle.eval(p[None]), FP64_BIN_REL, FP64_LLH_ABS, f"point {i}")
@@ -76,10 +89,11 @@ def test_c1_fp32_plain(c1, c1_oracle):
     eng.close()
 
 
-def test_c1_thousand_points_fp64(c1, c1_oracle):
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_c1_thousand_points(c1, c1_oracle, precision):
     """C1's stated result: Poisson LLH and bin contents at 1000 random
-    parameter points, FP64, in four batched launches of 250 points."""
-    eng = Engine.from_workload(c1, precision="fp64", k_max=250, llh_type=N.GW_LLH_POISSON)
+    parameter points, in four batched launches of 250 points."""
+    eng = Engine.from_workload(c1, precision=precision, k_max=250, llh_type=N.GW_LLH_POISSON)
     pts = c1.draw_points(1000, 1000)
     ref = c1_oracle.eval(pts)
     parts = [eng.eval(pts[a:a + 250]) for a in range(0, 1000, 250)]
@@ -88,13 +102,13 @@ def test_c1_thousand_points_fp64(c1, c1_oracle):
     eng.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "df64"])
 @pytest.mark.parametrize("K", [2, 4, 16, 64, 200, 256])
 def test_c1_batched(c1, c1_oracle, precision, K):
     eng = Engine.from_workload(c1, precision=precision, k_max=256, llh_type=N.GW_LLH_POISSON)
     pts = c1.draw_points(K, 100 + K)
     ref = c1_oracle.eval(pts)
-    rel, ab = (FP64_BIN_REL, FP64_LLH_ABS) if precision == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
+    rel, ab = _tol(precision)
     _check(eng.eval(pts), ref, rel, ab, f"K={K}")
     eng.close()
 
@@ -111,10 +125,11 @@ def test_batched_point_equals_plain_point(c1):
     eng.close()
 
 
-def test_mixed_all_dial_types_fp64(mixed, mixed_oracle):
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_mixed_all_dial_types(mixed, mixed_oracle, precision):
     """Every dial type, mirrored and truncated parameters, response clamps, the
     weight cap, host tables, base weights != 1, events without dials and empty bins."""
-    eng = Engine.from_workload(mixed, precision="fp64", k_max=8, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    eng = Engine.from_workload(mixed, precision=precision, k_max=8, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
     eng.set_event_weight_copy(True)
     pts = np.vstack([mixed.nominal(), mixed.draw_points(15, 9, inflate=1.6)])
     for i, p in enumerate(pts):
@@ -122,7 +137,7 @@ def test_mixed_all_dial_types_fp64(mixed, mixed_oracle):
         out = eng.eval(p[None])
         _check(out, ref, FP64_BIN_REL, FP64_LLH_ABS, f"point {i}")
         w = eng.event_weights()
-        assert _bin_rel(w, ref["weights"]) <= 1e-13
+        assert _bin_rel(w, ref["weights"]) <= (1e-13 if precision == "fp64" else DF64_EVENT_REL)
         counts = np.bincount(mixed.event_bin, minlength=mixed.n_bins)
         assert np.any(counts == 0) and np.all(out[0][0][counts == 0] == 0.0)
     _check(eng.eval(pts[:8]), mixed_oracle.eval(pts[:8]), FP64_BIN_REL, FP64_LLH_ABS, "batched")
@@ -255,7 +270,7 @@ def _extrapolation_factor(t, d, x, y):
     return ((1 + fx) * (1 + fy)) ** 3
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "df64"])
 def test_reference_golden_dials_through_engine(precision):
     """One event per golden case, one dial per event, on its own parameter(s);
     the event weight is the dial response computed by the reference's own
@@ -291,6 +306,8 @@ def test_reference_golden_dials_through_engine(precision):
         amp = np.array([_extrapolation_factor(c[0], data[c[1]], c[2], c[3]) for c in part])
         if precision == "fp64":
             tol = 1e-13 * np.maximum(1.0, np.abs(ref)) * amp
+        elif precision == "df64":
+            tol = 1e-12 * np.maximum(1.0, np.abs(ref)) * amp
         else:
             tol = 1e-4 * np.maximum(1.0, np.abs(ref)) * amp
         bad = np.nonzero(np.abs(w - ref) > tol)[0]
@@ -298,7 +315,7 @@ def test_reference_golden_dials_through_engine(precision):
         eng.close()
 
 
-def test_c2_subset_fp64_and_fp32():
+def test_c2_subset_all_precisions():
     wl = Workload("c2", n_events=300000, seed=21)
     orc = Oracle(wl, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
     pts = np.vstack([wl.nominal(), wl.draw_points(5, 2)])
@@ -311,6 +328,11 @@ def test_c2_subset_fp64_and_fp32():
     e32 = Engine.from_workload(wl, precision="fp32", k_max=8)
     _check(e32.eval(pts), ref, FP32_BIN_REL, FP32_LLH_ABS, "c2 fp32")
     e32.close()
+    edf = Engine.from_workload(wl, precision="df64", k_max=8)
+    _check(edf.eval(pts), ref, FP64_BIN_REL, FP64_LLH_ABS, "c2 df64 batched")
+    for i in range(2):
+        _check(edf.eval(pts[i:i + 1]), orc.eval(pts[i:i + 1]), FP64_BIN_REL, FP64_LLH_ABS, "c2 df64 plain")
+    edf.close()
 
 
 def test_device_pointer_entry_point(c1, c1_oracle):
@@ -341,7 +363,7 @@ def test_engine_matches_reference_cache_manager_fixtures(name, cfg, events):
     wl = Workload(cfg, n_events=events, seed=2)
     pts = g[f"{name}_points"]
     occ = np.bincount(wl.event_bin, minlength=wl.n_bins) > 0
-    for prec, tol in (("fp64", 1e-12), ("fp32", 2e-5)):
+    for prec, tol in (("fp64", 1e-12), ("fp32", 2e-5), ("df64", 1e-12)):
         eng = Engine.from_workload(wl, precision=prec, k_max=len(pts))
         s, s2, _, _ = eng.eval(pts)
         for got, ref in ((s, g[f"{name}_sums"]), (s2, g[f"{name}_sums2"])):
@@ -351,7 +373,7 @@ def test_engine_matches_reference_cache_manager_fixtures(name, cfg, events):
         eng.close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
 def test_both_k1_kernels_agree_bit_for_bit(mixed, prec):
     """k_plain and the warp-specialised k_plain_ws form the same products and
     sums in the same order: identical results, per-event weights included;
@@ -395,7 +417,7 @@ def test_eigen_decomposed_parameters(c1, c1_oracle):
     e2.close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
 def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
     """Every compiled batched kernel shape (both families, every register
     target) on the workload with every dial type, K = 64 inflated prior draws
@@ -405,7 +427,7 @@ def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
     eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
     pts = mixed.draw_points(K, 77, inflate=2.5)
     ref = mixed_oracle.eval(pts)
-    tol = (FP64_BIN_REL, FP64_LLH_ABS) if prec == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
+    tol = _tol(prec)
     first = {}
     tried = 0
     for i, (kind, ppp, ppt, threads, stages, minb) in enumerate(Engine.compiled_shapes()):
