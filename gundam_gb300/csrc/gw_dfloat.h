@@ -15,9 +15,13 @@
 //   two_sum(a, b)      = (s, e), s = fl(a + b), a + b = s + e exactly;
 //   fast_two_sum(a, b) = the same when |a| >= |b| (three operations);
 //   a * b              = p + e with p = fl(a * b), e = fma(a, b, -p).
-// Sums and products of two double-floats carry a relative error of a few
+// A sum adds the low words together and carries the high words' exact
+// rounding error (the "sloppy" sum of the double-double literature): its
+// error is a few units of 2^-48 of the larger operand, which is what the
+// reweighting needs (every value is a bounded combination of stored
+// coefficients of similar size); a product carries a relative error of a few
 // units of 2^-48 (about 1e-14); a quotient is formed from three corrected
-// partial quotients.
+// partial quotients.  Scaling by a power of two is exact (df_scale).
 #pragma once
 #include <cmath>
 
@@ -74,13 +78,9 @@ __device__ __forceinline__ dfloat df_fast_two_sum(float a, float b) {
 
 __device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
 
-// Sum with both the high and the low words' rounding errors carried (accurate
-// also when the operands cancel).
 __device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
-  dfloat s = df_two_sum(a.hi, b.hi);
-  const dfloat t = df_two_sum(a.lo, b.lo);
-  s = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
-  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+  const dfloat s = df_two_sum(a.hi, b.hi);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 __device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
 
@@ -91,6 +91,8 @@ __device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
   e = __fmaf_rn(a.lo, b.hi, e);
   return df_fast_two_sum(p, e);
 }
+// Exact product with a power of two.
+__device__ __forceinline__ dfloat df_scale(dfloat a, float pow2) { return dfloat(a.hi * pow2, a.lo * pow2); }
 // Product with a single float (its low word zero).
 __device__ __forceinline__ dfloat df_mul_f(dfloat a, float b) {
   const float p = __fmul_rn(a.hi, b);

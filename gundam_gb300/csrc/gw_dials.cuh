@@ -33,6 +33,16 @@ __device__ __forceinline__ T hermite(T p1, T m1, T p2, T m2, T fx) {
            m1) * fx + p1);
 }
 
+// The same cubic in double-float arithmetic, written p1 + fx(m1 + fx(B + fx A))
+// with A = m1 + m2 - 2 dc, B = 3 dc - 2 m1 - m2, dc = p2 - p1, the doublings
+// exact: 9 double-float sums and products instead of the 19 of the form above.
+__device__ __forceinline__ dfloat hermite(dfloat p1, dfloat m1, dfloat p2, dfloat m2, dfloat fx) {
+  const dfloat dc = p2 - p1;
+  const dfloat a = (m1 + m2) - df_scale(dc, 2.0f);
+  const dfloat b = (df_mul_f(dc, 3.0f) - df_scale(m1, 2.0f)) - m2;
+  return p1 + fx * (m1 + fx * (b + fx * a));
+}
+
 // Hermite spline on non-uniform knots: CalculateGeneralSpline.h:51-197, with
 // its 5-step branch-free search (:135-159).  Here the payload drops the unused
 // [low, step] prefix: d = [(y, dydx, x) x n].

@@ -288,7 +288,7 @@ def main():
     ap.add_argument("--n-sub", type=int, default=10)
     ap.add_argument("--nodes", type=int, default=8)
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "df64"])
     ap.add_argument("--region", default="posterior", choices=["posterior", "prior"])
     ap.add_argument("--proposal", default="adapted", choices=["adapted", "prior"])
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -298,13 +298,15 @@ def main():
     ap.add_argument("--eps", type=float, default=0.25)
     ap.add_argument("--n-leap", type=int, default=10)
     ap.add_argument("--no-linear", action="store_true")
+    ap.add_argument("--base-only-steps", type=int, default=0)
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args()
     lg = (lambda m: print(m, file=sys.stderr, flush=True)) if a.verbose else None
     print(json.dumps(run(a.events, a.train, a.epochs, a.chains, a.steps, a.n_sub, config=a.config,
                          precision=a.precision, region=a.region, proposal=a.proposal, nodes=a.nodes,
                          linear=not a.no_linear, log=lg, da_steps=a.da_steps or None, lr=a.lr, thin=a.thin,
-                         warm_steps=a.warm_steps, stage1=a.stage1, eps=a.eps, n_leap=a.n_leap)))
+                         warm_steps=a.warm_steps, stage1=a.stage1, eps=a.eps, n_leap=a.n_leap,
+                         base_only_steps=a.base_only_steps or None)))
 
 
 if __name__ == "__main__":

@@ -447,7 +447,7 @@ def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
         else:
             first[key] = out
         tried += 1
-    assert tried >= 10
+    assert tried >= (5 if prec == "df64" else 10)  # double-float is compiled for five shapes
     eng.close()
 
 
