@@ -504,6 +504,22 @@ def run_gw(args, world, rank, local, dist):
                 eng.autotune(K)
                 msk, kmsk, _ = time_device(eng, torch, d, K, min(args.steps, 20), args.warmup, dist)
                 variants[f"fp64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk}
+            # the same in double-float (two FP32 words per value on the FP32
+            # pipe, sums and LLH in FP64; held to the FP64 parity bar)
+            eng.close()
+            eng = Engine.from_workload(wl, precision="df64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
+                                       device=local)
+            eng.autotune(1)
+            msd, kmsd, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
+            algd = algorithmic_bytes(wl, "df64", 1)
+            variants["df64_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
+                "evals_per_s": 1e3 / msd, "ms_per_eval": msd, "kernel_ms": kmsd,
+                "kernel_gbs": algd / (kmsd / 1e3) / 1e9, "kernel_frac_of_hbm_peak": algd / (kmsd / 1e3) / 1e9 / peak}
+            if K > 1:
+                eng.autotune(K)
+                msk, kmsk, _ = time_device(eng, torch, d, K, min(args.steps, 20), args.warmup, dist)
+                variants[f"df64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk,
+                                          "shape": list(Engine.compiled_shapes()[eng.shape_index()])}
             if K < 256:
                 eng.close()
                 K2 = 256
