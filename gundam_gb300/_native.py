@@ -37,6 +37,7 @@ GW_FP32 = 1
 GW_DF64 = 2
 GW_FLAG_SPLINE_KNOTS = 1
 GW_FLAG_SPLINE_SLOPES = 2
+GW_FLAG_SPLINE_COEFS = 3
 
 GW_LLH_NONE = 0
 GW_LLH_POISSON = 1

@@ -116,6 +116,20 @@ __device__ __forceinline__ void issue_tile_hdr(const DevView& v, int tile, unsig
 // ---------------------------------------------------------------------------
 // Uniform-knot splines with stored slopes at KR points: in FP32 with an even
 // KR, pairs of points go through the packed-FP32 evaluator.
+// Uniform-knot splines in the coefficient form at KR points: pairs of points
+// in packed FP32 when T is float and KR even.
+template <typename T, int KR>
+__device__ __forceinline__ void coef_values(const T* __restrict__ d, int n, const T (&x)[KR], bool trunc,
+                                            T (&val)[KR]) {
+  if constexpr (sizeof(T) == 4 && KR % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KR; j += 2) eval_coef2(d, n, x[j], x[j + 1], trunc, val[j], val[j + 1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < KR; ++j) val[j] = eval_coef<T>(d, n, x[j], trunc);
+  }
+}
+
 template <typename T, bool catmull, int KR>
 __device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, const T (&x)[KR], bool trunc,
                                                 T (&val)[KR]) {
@@ -213,7 +227,9 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       // clamps are one clamp to the intersection.
       if (lo < T(-1e20)) lo = T(-1e20);
       if (hi > T(1e20)) hi = T(1e20);
-      if (type == kMonotonic) {
+      if (v.spline_coefs && (type == kMonotonic || type == kUniform || type == kCompact)) {
+        coef_values<T, KR>(d, n, x, trunc, val);
+      } else if (type == kMonotonic) {
         if (v.spline_knots) {
 #pragma unroll
           for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, true>(d, n, x[j], trunc);

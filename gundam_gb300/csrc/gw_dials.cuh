@@ -279,6 +279,63 @@ __device__ __forceinline__ void eval_prepared2(const float* __restrict__ d, int 
   upk2(fma2(fma2(fma2(a, fx, b), fx, m1), fx, p1), va, vb);
 }
 
+// Uniform-knot splines in the coefficient form (GW_FLAG_SPLINE_COEFS):
+// d = [-low/step, 1/step, 0, 0, (c0, c1, c2, c3) x (n + 1)].  xx = (x - low)
+// / step as one multiply-add, j = clamp(floor(xx), -1, n - 1), u = xx - j,
+// and the block j + 1 holds the cubic of u on that interval (the blocks of
+// j = -1 and j = n - 1 hold the reference's extrapolation beyond the first and
+// the last knot, re-expanded about their own origin), so no end rule is
+// applied here.  With truncation xx is first clamped to [0, n - 1] (the end
+// knots' values).  The coefficient blocks are 16-byte aligned.
+template <typename T>
+__device__ __forceinline__ T eval_coef(const T* __restrict__ d, int n, T x, bool trunc) {
+  T xx = x * d[1] + d[0];
+  if (trunc) xx = (xx < T(0)) ? T(0) : ((xx > T(n - 1)) ? T(n - 1) : xx);
+  int j;
+  T fj;
+  if constexpr (sizeof(T) == 4) {
+    const float f = __fadd_rd(xx, 12582912.0f) - 12582912.0f;  // floor, as knot_interval
+    const float nm1 = __int_as_float(0x4B000000 | (n - 1)) - 8388608.0f;
+    fj = fminf(fmaxf(f, -1.0f), nm1);
+    j = __float_as_int(fj + 8388609.0f) - 0x4B000000;  // j + 1
+  } else {
+    const T xc = (xx < T(-1)) ? T(-1) : ((xx > T(n - 1)) ? T(n - 1) : xx);
+    int i = (int)xc;     // truncation, in [-1, n - 1]
+    if (T(i) > xc) --i;  // floor
+    fj = T(i);
+    j = i + 1;
+  }
+  const T u = xx - fj;
+  const T* c = d + 4 + 4 * j;
+  return c[0] + u * (c[1] + u * (c[2] + u * c[3]));
+}
+
+// The same at two points (FP32): one 16-byte load per point, the index and
+// the cubic in packed FP32.
+__device__ __forceinline__ void eval_coef2(const float* __restrict__ d, int n, float xa, float xb, bool trunc,
+                                           float& va, float& vb) {
+  f32x2 xx = fma2(pk2(xa, xb), pk2(d[1], d[1]), pk2(d[0], d[0]));
+  const float nm1 = __int_as_float(0x4B000000 | (n - 1)) - 8388608.0f;  // (float)(n - 1)
+  if (trunc) {
+    float a, b;
+    upk2(xx, a, b);
+    xx = pk2(fminf(fmaxf(a, 0.0f), nm1), fminf(fmaxf(b, 0.0f), nm1));
+  }
+  const f32x2 magic = pk2(12582912.0f, 12582912.0f);
+  float fa, fb;
+  upk2(sub2(add2_rm(xx, magic), magic), fa, fb);
+  fa = fminf(fmaxf(fa, -1.0f), nm1);
+  fb = fminf(fmaxf(fb, -1.0f), nm1);
+  const f32x2 fj = pk2(fa, fb);
+  float ba, bb;
+  upk2(add2(fj, pk2(8388609.0f, 8388609.0f)), ba, bb);
+  const float4 ca = *(const float4*)(d + 4 + 4 * (__float_as_int(ba) - 0x4B000000));
+  const float4 cb = *(const float4*)(d + 4 + 4 * (__float_as_int(bb) - 0x4B000000));
+  const f32x2 u = sub2(xx, fj);
+  const f32x2 v = fma2(fma2(fma2(pk2(ca.w, cb.w), u, pk2(ca.z, cb.z)), u, pk2(ca.y, cb.y)), u, pk2(ca.x, cb.x));
+  upk2(v, va, vb);
+}
+
 // Index of the facet for a value: BilinearIndex / BicubicIndex
 // (CalculateBilinearInterpolation.h:36-60), restricted to in-range reads.
 template <typename T>

@@ -224,7 +224,8 @@ extern "C" int gw_create(const gw_config* c, gw_engine** out) {
   *out = nullptr;
   if (c->n_results < 0 || c->n_params < 1 || c->n_params > 8192 || c->n_bins < 1 || c->k_max < 1 ||
       c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32 && c->precision != GW_DF64) ||
-      (c->flags != 0 && c->flags != GW_FLAG_SPLINE_KNOTS && c->flags != GW_FLAG_SPLINE_SLOPES))
+      (c->flags != 0 && c->flags != GW_FLAG_SPLINE_KNOTS && c->flags != GW_FLAG_SPLINE_SLOPES &&
+       c->flags != GW_FLAG_SPLINE_COEFS))
     return fail(nullptr, GW_ERR_ARG,
                 "bad gw_config (n_results=%d n_params=%d n_bins=%d k_max=%d precision=%d flags=%d)",
                 c->n_results, c->n_params, c->n_bins, c->k_max, c->precision, c->flags);
@@ -659,55 +660,112 @@ void write_payload(const DialRec& r, const double* d, T* out) {
   }
 }
 
-// Engine layout of Catmull-Rom (monotonic, compact) and uniform splines:
-// [low, 1/step, (y, s) x n] with s the knot slope in index units.  The
-// Catmull-Rom slope of knot k is the one CalculateMonotonicSpline.h:66-127
-// forms from its neighbours (with the Fritsch-Carlson limiter for monotonic
-// splines); the end knots get the end difference.  Computed here in FP64.
+// Knot values and slopes in index units of a uniform-knot spline: for
+// uniform splines the stored dydx times the step; for Catmull-Rom splines the
+// slope CalculateMonotonicSpline.h:66-127 forms from the neighbours (with the
+// Fritsch-Carlson limiter for monotonic splines), the end knots the end
+// difference.  In FP64.
+static void knot_slopes(const DialRec& r, const double* d, int n, double* y, double* s) {
+  const double step = d[1];
+  if (r.type == kUniform) {
+    for (int k = 0; k < n; ++k) {
+      y[k] = d[2 + 2 * k];
+      s[k] = d[3 + 2 * k] * step;
+    }
+    return;
+  }
+  const bool limit = r.type == kMonotonic;
+  for (int k = 0; k < n; ++k) y[k] = d[2 + k];
+  for (int k = 0; k < n; ++k) {
+    if (k == 0) {
+      s[k] = y[1] - y[0];
+    } else if (k == n - 1) {
+      s[k] = y[n - 1] - y[n - 2];
+    } else {
+      const double dl = y[k] - y[k - 1], dr = y[k + 1] - y[k];
+      double v = 0.5 * (dl + dr);
+      if (limit) {
+        if (dr * dl <= 0.0) v = 0.0;
+        const double delta = 3.0 * std::min(std::fabs(dl), std::fabs(dr));
+        if (v > delta) v = delta;
+        if (v < -delta) v = -delta;
+      }
+      s[k] = v;
+    }
+  }
+}
+
+// Stored form of a spline's Catmull-Rom or Hermite data (SplineForm).
+enum SplineForm { kFormSlopes = 0, kFormKnots = 1, kFormCoefs = 2 };
+
+// Engine layout of Catmull-Rom (monotonic, compact) and uniform splines.
+// Slopes form: [low, 1/step, (y, s) x n], s the knot slope in index units
+// (knot_slopes); knots form (Catmull-Rom only): [low, 1/step, y x n], the
+// slopes formed in the kernel; coefficients form: below.
 template <typename T>
-void write_prepared(const DialRec& r, const double* d, int n, T* out, bool knots) {
+void write_prepared(const DialRec& r, const double* d, int n, T* out, int form) {
   const double low = d[0], step = d[1];
+  if (form == kFormCoefs) {
+    // [-low/step, 1/step, 0, 0, (c0, c1, c2, c3) x (n + 1)]: interval j + 1
+    // holds the cubic v(u) = c0 + u (c1 + u (c2 + u c3)) of u = xx - j, xx =
+    // (x - low) / step, for j = -1 .. n - 1.  j = 0 .. n - 2 are the Hermite
+    // cubics on the knot intervals (CalculateUniformSpline.h:71-74 expanded);
+    // j = -1 and j = n - 1 re-expand the end intervals' cubics, which the
+    // reference evaluates beyond the knots (for Catmull-Rom splines with the
+    // end difference as the outer slope, CalculateMonotonicSpline.h:66-103),
+    // about u = xx + 1 and u = xx - (n - 1).
+    std::vector<double> y((size_t)n), sl((size_t)n);
+    knot_slopes(r, d, n, y.data(), sl.data());
+    const bool catmull = r.type != kUniform;
+    auto cubic = [&](int i, double m1, double m2, double* c) {
+      const double dc = y[(size_t)i + 1] - y[(size_t)i];
+      c[0] = y[(size_t)i];
+      c[1] = m1;
+      c[2] = 3.0 * dc - 2.0 * m1 - m2;
+      c[3] = m1 + m2 - 2.0 * dc;
+    };
+    out[0] = (T)(-low / step);
+    out[1] = (T)(1.0 / step);
+    out[2] = (T)0.0;
+    out[3] = (T)0.0;
+    double c[4];
+    for (int j = 0; j + 1 < n; ++j) {
+      cubic(j, sl[(size_t)j], sl[(size_t)j + 1], c);
+      for (int q = 0; q < 4; ++q) out[4 + 4 * (j + 1) + q] = (T)c[q];
+    }
+    // before the first knot: P(t), t = xx, as P(u - 1)
+    cubic(0, sl[0], catmull ? y[1] - y[0] : sl[1], c);
+    const double left[4] = {c[0] - c[1] + c[2] - c[3], c[1] - 2.0 * c[2] + 3.0 * c[3], c[2] - 3.0 * c[3], c[3]};
+    // after the last knot: P(t), t = xx - (n - 2), as P(u + 1)
+    cubic(n - 2, catmull ? y[(size_t)n - 1] - y[(size_t)n - 2] : sl[(size_t)n - 2], sl[(size_t)n - 1], c);
+    const double right[4] = {c[0] + c[1] + c[2] + c[3], c[1] + 2.0 * c[2] + 3.0 * c[3], c[2] + 3.0 * c[3], c[3]};
+    for (int q = 0; q < 4; ++q) {
+      out[4 + q] = (T)left[q];
+      out[4 + 4 * n + q] = (T)right[q];
+    }
+    return;
+  }
   out[0] = (T)low;
   out[1] = (T)(1.0 / step);
-  if (knots && r.type != kUniform) {  // [low, 1/step, y x n]: slopes formed in the kernel
+  if (form == kFormKnots && r.type != kUniform) {  // [low, 1/step, y x n]: slopes formed in the kernel
     for (int k = 0; k < n; ++k) out[2 + k] = (T)d[2 + k];
     return;
   }
-  if (r.type == kUniform) {
-    for (int k = 0; k < n; ++k) {
-      out[2 + 2 * k] = (T)d[2 + 2 * k];
-      out[3 + 2 * k] = (T)(d[3 + 2 * k] * step);
-    }
-    return;
-  }
-  const double* y = d + 2;
-  const bool limit = r.type == kMonotonic;
+  std::vector<double> y((size_t)n), sl((size_t)n);
+  knot_slopes(r, d, n, y.data(), sl.data());
   for (int k = 0; k < n; ++k) {
-    double s;
-    if (k == 0) {
-      s = y[1] - y[0];
-    } else if (k == n - 1) {
-      s = y[n - 1] - y[n - 2];
-    } else {
-      const double dl = y[k] - y[k - 1], dr = y[k + 1] - y[k];
-      s = 0.5 * (dl + dr);
-      if (limit) {
-        if (dr * dl <= 0.0) s = 0.0;
-        const double delta = 3.0 * std::min(std::fabs(dl), std::fabs(dr));
-        if (s > delta) s = delta;
-        if (s < -delta) s = -delta;
-      }
-    }
-    out[2 + 2 * k] = (T)y[k];
-    out[3 + 2 * k] = (T)s;
+    out[2 + 2 * k] = (T)y[(size_t)k];
+    out[3 + 2 * k] = (T)sl[(size_t)k];
   }
 }
 
 // Stored elements of a dial in the engine precision.  Non-empty payloads are
 // padded to an odd element count: threads that read consecutive same-type
 // dials then hit distinct shared-memory banks.
-int32_t stored_elems(const DialRec& r, int n, int32_t raw, bool knots) {
-  int32_t el = (r.type == kMonotonic || r.type == kCompact) ? (knots ? 2 + n : 2 + 2 * n) : raw;
+int32_t stored_elems(const DialRec& r, int n, int32_t raw, int form) {
+  const bool uniform_knots = r.type == kMonotonic || r.type == kCompact || r.type == kUniform;
+  if (form == kFormCoefs && uniform_knots) return 4 + 4 * (n + 1);  // 16-byte multiple, packed first
+  int32_t el = (r.type == kMonotonic || r.type == kCompact) ? (form == kFormKnots ? 2 + n : 2 + 2 * n) : raw;
   if (el > 0 && (el & 1) == 0) ++el;
   return el;
 }
@@ -730,8 +788,10 @@ int build_and_upload(gw_engine* e) {
   const size_t tsz = sizeof(T);
   // stored form of Catmull-Rom splines (gw_config.flags; by default knot
   // values for FP32 K = 1 engines, precomputed slopes otherwise)
-  const bool knots = e->cfg.flags == GW_FLAG_SPLINE_KNOTS ||
-                     (e->cfg.flags == 0 && e->cfg.k_max == 1 && tsz == 4);
+  const int form = e->cfg.flags == GW_FLAG_SPLINE_KNOTS  ? kFormKnots
+                   : e->cfg.flags == GW_FLAG_SPLINE_COEFS ? kFormCoefs
+                   : (e->cfg.flags == 0 && e->cfg.k_max == 1 && tsz == 4) ? kFormKnots
+                                                                           : kFormSlopes;
 
   // 1. every result needs a bin (CacheManager.cpp:727-729 "Histogram cells are missing")
   for (int r = 0; r < N; ++r)
@@ -770,7 +830,7 @@ int build_and_upload(gw_engine* e) {
             int64_t exp = -1;
             bad.compare_exchange_strong(exp, i);
           }
-          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, knots);
+          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, form);
           pn[(size_t)i] = n;
         }
       });
@@ -904,9 +964,14 @@ int build_and_upload(gw_engine* e) {
           const int nd = (int)ev_major.size();
           order.resize(nd);
           for (int s = 0; s < nd; ++s) order[s] = s;
-          std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            return e->dials[(size_t)ev_major[a]].type < e->dials[(size_t)ev_major[b]].type;
-          });
+          // type order; in the coefficient form the three uniform-knot spline
+          // types first, so their 16-byte-multiple payloads start 16-byte aligned
+          auto key = [&](int a) {
+            const int ty = e->dials[(size_t)ev_major[a]].type;
+            const bool first = form == kFormCoefs && (ty == kMonotonic || ty == kCompact || ty == kUniform);
+            return (first ? 0 : 16) + ty;
+          };
+          std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
           T* pl = (T*)(payload.data() + tp.payload_off);
           int off = 0;
           for (int j = 0; j < nd; ++j) {
@@ -917,7 +982,7 @@ int build_and_upload(gw_engine* e) {
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
             hdr[(size_t)(tp.dial0 + j)] = make_header(r.type, pn[(size_t)di], slot, off, p0, p1);
             if (r.type == kMonotonic || r.type == kCompact || r.type == kUniform)
-              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off, knots);
+              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off, form);
             else
               write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
             off += pel[(size_t)di];
@@ -989,7 +1054,8 @@ int build_and_upload(gw_engine* e) {
   v.cap = e->cap;
   v.tile_payload_bytes = (int)(((cap_elems * tsz) + 127) & ~(int64_t)127);
   v.tile_hdr_bytes = std::max(16, ((max_tile_dials + 1) / 2) * 16);
-  v.spline_knots = knots ? 1 : 0;
+  v.spline_knots = form == kFormKnots ? 1 : 0;
+  v.spline_coefs = form == kFormCoefs ? 1 : 0;
 
   // slack after the per-dial and per-event arrays (reads rounded out to
   // 16-byte boundaries stay inside the allocation)

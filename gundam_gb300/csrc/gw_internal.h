@@ -30,6 +30,7 @@ struct DevView {
   int tile_payload_bytes;  // shared-memory bytes reserved per payload stage
   int tile_hdr_bytes;      // shared-memory bytes for one tile's headers (16-byte multiple)
   int spline_knots;        // 1: Catmull-Rom payloads hold knot values only (slopes formed on the device)
+  int spline_coefs;        // 1: monotonic, compact and uniform splines hold per-interval cubic coefficients
   double cap;
 
   const TileDesc* tiles;

@@ -25,11 +25,14 @@ def _c(a, dtype):
 class Engine:
     def __init__(self, n_results: int, n_params: int, n_bins: int, k_max: int = 1, precision: str = "fp64",
                  device: int = 0, tile_bytes: int = 0, spline_layout: str = "auto"):
-        """spline_layout: stored form of Catmull-Rom splines, "knots" (knot
-        values, slopes formed on the device), "slopes" (slopes precomputed on
-        the host) or "auto" (knots for an FP32 engine with k_max == 1)."""
+        """spline_layout: stored form of the uniform-knot splines, "knots"
+        (Catmull-Rom knot values, slopes formed on the device), "slopes"
+        (slopes precomputed on the host), "coefs" (per-interval cubic
+        coefficients, extrapolation intervals included) or "auto" (knots for
+        an FP32 engine with k_max == 1, slopes otherwise)."""
         self.lib = N.libgw()
-        flags = {"auto": 0, "knots": N.GW_FLAG_SPLINE_KNOTS, "slopes": N.GW_FLAG_SPLINE_SLOPES}[spline_layout]
+        flags = {"auto": 0, "knots": N.GW_FLAG_SPLINE_KNOTS, "slopes": N.GW_FLAG_SPLINE_SLOPES,
+                 "coefs": N.GW_FLAG_SPLINE_COEFS}[spline_layout]
         prec = {"fp32": N.GW_FP32, "fp64": N.GW_FP64, "df64": N.GW_DF64}[precision]
         cfg = N.GwConfig(int(n_results), int(n_params), int(n_bins), int(k_max), prec, int(device), int(tile_bytes),
                          flags)

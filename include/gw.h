@@ -81,7 +81,16 @@ enum {
  * grouping of their FP64 partial sums, as the tiles are cut differently). */
 enum {
   GW_FLAG_SPLINE_KNOTS = 1,
-  GW_FLAG_SPLINE_SLOPES = 2
+  GW_FLAG_SPLINE_SLOPES = 2,
+  /* Monotonic, compact and uniform splines stored per interval as the
+   * power-basis coefficients of the cubic the reference evaluates there,
+   * [-low/step, 1/step, 0, 0, (c0, c1, c2, c3) x (n + 1)], with one interval
+   * before the first knot and one after the last holding the reference's
+   * extrapolation (for Catmull-Rom splines the end difference as the outer
+   * slope): one 16-byte load and three multiply-adds per point, about 2.2x
+   * the bytes of the slope form.  For batched evaluation, where the
+   * arithmetic, not the bytes, bounds the kernel. */
+  GW_FLAG_SPLINE_COEFS = 3
 };
 
 /* ---- likelihood evaluated after the histogram step --------------------- */

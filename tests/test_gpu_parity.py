@@ -417,14 +417,16 @@ def test_eigen_decomposed_parameters(c1, c1_oracle):
     e2.close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
-def test_every_compiled_batched_shape(mixed, mixed_oracle, prec):
-    """Every compiled batched kernel shape (both families, every register
+@pytest.mark.parametrize("prec,layout", [("fp64", "auto"), ("fp32", "auto"), ("df64", "auto"), ("fp32", "coefs")])
+def test_every_compiled_batched_shape(mixed, mixed_oracle, prec, layout):
+    """Every compiled batched kernel shape (every family, every register
     target) on the workload with every dial type, K = 64 inflated prior draws
     (extrapolation beyond the knot ranges included), against the oracle; the
-    register targets of one shape give identical results."""
+    register targets of one shape give identical results.  Also with the
+    uniform-knot splines in the coefficient form."""
     K = 64
-    eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021,
+                               spline_layout=layout)
     pts = mixed.draw_points(K, 77, inflate=2.5)
     ref = mixed_oracle.eval(pts)
     tol = _tol(prec)
@@ -471,18 +473,20 @@ def test_shape_that_overruns_the_padded_points_is_refused(c1, c1_oracle):
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_spline_layouts_agree(mixed, mixed_oracle, prec):
     """Catmull-Rom splines stored as knot values (the slopes formed on the
-    device) or with slopes precomputed on the host: both within tolerance of
-    the oracle through the K = 1 and the batched kernels.  In FP64 the
-    per-event weights are identical; the bin sums differ only in rounding,
-    because the smaller payload cuts different tiles and so groups the FP64
-    partial sums differently.  The knot form packs fewer bytes, and an FP32
-    K = 1 engine picks it."""
+    device), with slopes precomputed on the host, or all uniform-knot splines
+    as per-interval cubic coefficients (extrapolation intervals included):
+    each within tolerance of the oracle through the K = 1 and the batched
+    kernels, with draws far enough out to extrapolate.  In FP64 the knot and
+    slope forms give identical per-event weights; the bin sums differ only in
+    rounding, because the smaller payload cuts different tiles and so groups
+    the FP64 partial sums differently.  The knot form packs fewer bytes, and
+    an FP32 K = 1 engine picks it."""
     llh = N.GW_LLH_BARLOW_BEESTON_OA2021
     pts = mixed.draw_points(4, 61, inflate=2.0)
     ref = mixed_oracle.eval(pts)
     tol = (FP64_BIN_REL, FP64_LLH_ABS) if prec == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
     out = {}
-    for layout in ("knots", "slopes"):
+    for layout in ("knots", "slopes", "coefs"):
         eng = Engine.from_workload(mixed, precision=prec, k_max=4, llh_type=llh, spline_layout=layout)
         eng.set_event_weight_copy(True)
         weights = []
