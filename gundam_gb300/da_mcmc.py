@@ -260,6 +260,15 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
             "mean_diff_over_mc_se_rms": float(np.sqrt(np.mean((mean_diff / se) ** 2))),
             "width_ratio_range": [float((sig_d / sig_p).min()), float((sig_d / sig_p).max())],
             "width_ratio_median": float(np.median(sig_d / sig_p)),
+            # resolution: the Monte Carlo standard error of the mean difference
+            # in units of sigma, and of the relative width difference (a width
+            # estimated from ESS draws has relative error ~ 1 / sqrt(2 ESS))
+            "mean_diff_mc_se_over_sigma_median": float(np.median(se / sig_p)),
+            "mean_diff_mc_se_over_sigma_max": float((se / sig_p).max()),
+            "width_diff_over_sigma_max": float((np.abs(sig_d - sig_p) / sig_p).max()),
+            "width_diff_mc_se_median": float(np.median(np.sqrt(0.5 / ess_p + 0.5 / ess_d))),
+            "width_diff_over_mc_se_max": float((np.abs(sig_d - sig_p) / sig_p /
+                                               np.sqrt(0.5 / ess_p + 0.5 / ess_d)).max()),
         },
         "ess_per_s_gain_min": st_d["ess_per_s_min"] / st_p["ess_per_s_min"],
         "ess_per_s_gain_median": st_d["ess_per_s_median"] / st_p["ess_per_s_median"],
