@@ -466,25 +466,30 @@ def run_gw(args, world, rank, local, dist):
             "kernel_frac_of_hbm_peak": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9 / peak,
             "payload_bytes": e1.layout()["payload_bytes"], "spline_layout": "knots"}
         e1.close()
+        # small K: an engine sized for it (k_max = 4, its default spline form),
+        # the warp-specialised small-K kernels, autotuned; e2e through gw_eval
+        # with host buffers
+        es = Engine.from_workload(wl, precision=args.precision, k_max=4, llh_type=llh_type_for(args.config),
+                                  device=local)
         for Ks in (2, 4):
-            # small K: the warp-specialised small-K kernels, autotuned; e2e
-            # through gw_eval with host buffers
-            eng.autotune(Ks)
-            msk, kmsk, _ = time_device(eng, torch, d, Ks, args.steps, args.warmup, dist)
+            es.autotune(Ks)
+            msk, kmsk, _ = time_device(es, torch, d, Ks, args.steps, args.warmup, dist)
             pk = pts[:Ks]
             for _ in range(2):
-                eng.eval(pk)
+                es.eval(pk)
             t0 = time.perf_counter()
             for _ in range(args.steps):
-                eng.eval(pk)
+                es.eval(pk)
             e2e_k = (time.perf_counter() - t0) / args.steps
             algk = algorithmic_bytes(wl, args.precision, Ks)
-            sk = eng.shape_index()
+            sk = es.shape_index()
             variants[f"{args.precision}_K{Ks}"] = {
                 "shape": list(Engine.compiled_shapes()[sk]), "evals_per_s": Ks * 1e3 / msk, "ms_per_step": msk,
                 "kernel_ms": kmsk, "kernel_gbs": algk / (kmsk / 1e3) / 1e9,
                 "kernel_frac_of_hbm_peak": algk / (kmsk / 1e3) / 1e9 / peak,
-                "e2e_evals_per_s": Ks / e2e_k, "e2e_ms_per_step": e2e_k * 1e3}
+                "e2e_evals_per_s": Ks / e2e_k, "e2e_ms_per_step": e2e_k * 1e3,
+                "payload_bytes": es.layout()["payload_bytes"]}
+        es.close()
         if K > 16:
             # C3 at the C2 size: K = 16 on this engine, K = 256 on one sized for it
             eng.autotune(16)
