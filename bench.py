@@ -29,6 +29,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "LLH evals/s (5M events, C2 mixed dials)"
+# the K = 1 kernels by gw_get_plain_kernel value
+PLAIN_NAMES = ["k_plain", "k_plain_ws", "k_plain_ws (8 evaluator warps)"]
 
 
 def parse():
@@ -445,14 +447,14 @@ def run_gw(args, world, rank, local, dist):
     shape = eng.shape()
     sidx = eng.shape_index()
     sfull = Engine.compiled_shapes()[sidx] if sidx >= 0 else None
-    plain_name = ["k_plain", "k_plain_ws"][eng.plain_kernel()]
+    plain_name = PLAIN_NAMES[eng.plain_kernel()]
     variants = {}
     if not args.no_variants:
         # K = 1 (the plain kernel) on this engine, whose splines carry precomputed
         # slopes for the batched kernel, and on a K = 1 engine (knot values)
         eng.autotune(1)
         ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-        variants[f"{args.precision}_K1_slopes_layout"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
+        variants[f"{args.precision}_K1_slopes_layout"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
             "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9,
             "payload_bytes": layout["payload_bytes"]}
@@ -460,7 +462,7 @@ def run_gw(args, world, rank, local, dist):
                                   device=local)
         e1.autotune(1)
         ms1, kms1, _ = time_device(e1, torch, d, 1, args.steps, args.warmup, dist)
-        variants[f"{args.precision}_K1"] = {"kernel": ["k_plain", "k_plain_ws"][e1.plain_kernel()],
+        variants[f"{args.precision}_K1"] = {"kernel": PLAIN_NAMES[e1.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
             "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9,
             "kernel_frac_of_hbm_peak": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9 / peak,
@@ -502,7 +504,7 @@ def run_gw(args, world, rank, local, dist):
                                        device=local)
             eng.autotune(1)
             ms64, kms64, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-            variants["fp64_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
+            variants["fp64_K1"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
                 "evals_per_s": 1e3 / ms64, "ms_per_eval": ms64, "kernel_ms": kms64,
                 "kernel_gbs": algorithmic_bytes(wl, "fp64", 1) / (kms64 / 1e3) / 1e9}
             if K > 1:
@@ -517,7 +519,7 @@ def run_gw(args, world, rank, local, dist):
             eng.autotune(1)
             msd, kmsd, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
             algd = algorithmic_bytes(wl, "df64", 1)
-            variants["df64_K1"] = {"kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()],
+            variants["df64_K1"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
                 "evals_per_s": 1e3 / msd, "ms_per_eval": msd, "kernel_ms": kmsd,
                 "kernel_gbs": algd / (kmsd / 1e3) / 1e9, "kernel_frac_of_hbm_peak": algd / (kmsd / 1e3) / 1e9 / peak}
             if K > 1:

@@ -1466,7 +1466,7 @@ static int autotune_plain(gw_engine* e) {
   GW_CUDA(e, cudaEventCreate(&b));
   float best = 1e30f;
   int best_kind = e->view.plain_kind;
-  for (int kind = 0; kind < 2; ++kind) {
+  for (int kind = 0; kind < 3; ++kind) {
     if (gw_set_plain_kernel(e, kind) != GW_OK) continue;
     int rc = launch_chain(e, (const double*)e->d_params, 1, (double*)e->d_sums, (double*)e->d_sums2,
                           (double*)e->d_llh, (double*)e->d_llh_stat, e->stream);
@@ -1611,7 +1611,7 @@ extern "C" int gw_shape_at(int32_t i, int32_t* kind, int32_t* kc, int32_t* kr, i
 }
 
 extern "C" int gw_set_plain_kernel(gw_engine* e, int32_t kind) {
-  if (!e || kind < 0 || kind > 1) return GW_ERR_ARG;
+  if (!e || kind < 0 || kind > 2) return GW_ERR_ARG;
   if (!e->initialized) return fail(e, GW_ERR_STATE, "gw_initialize has not been called");
   GW_CUDA(e, cudaSetDevice(e->device));
   const int old = e->view.plain_kind;

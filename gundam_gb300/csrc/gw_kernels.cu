@@ -239,12 +239,15 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const DevView v) {
 // without work: no further copy is issued, no header is decoded, and before
 // the CTA exits thread 0 waits (bounded) for every copy still in flight.
 // ---------------------------------------------------------------------------
-constexpr int kWsEval = 192, kWsRed = 64;
+// NEV evaluator threads (192: six warps, the default; 256: eight warps, for
+// double-float, whose tiles hold fewer dials than one round of 192 threads
+// would cover evenly) and two reducer warps.
+constexpr int kWsRed = 64;
 constexpr int kBarEval = 1, kBarFull = 2, kBarEmpty = 4, kBarRed = 6;
 
-
-template <typename T>
-__global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain_ws(const DevView v) {
+template <typename T, int NEV>
+__global__ void __launch_bounds__(NEV + kWsRed, sizeof(T) == 4 ? 3 : 2) k_plain_ws(const DevView v) {
+  constexpr int kWsEval = NEV, NT = NEV + kWsRed;
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
   const int HB = v.tile_hdr_bytes;
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
         if (st) pend1 = -1;
         else pend0 = -1;
       }
-      if (it >= 2) named_sync(kBarEmpty + st, kPlainThreads);  // the reducers are done with buffer st
+      if (it >= 2) named_sync(kBarEmpty + st, NT);  // the reducers are done with buffer st
       T* dv = dval + st * 1024;
       // after any failed wait the stages hold nothing trustworthy: headers
       // are not decoded, so no shared-memory index comes from them
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
           dv[hdr_slot(h)] = val[0];
         }
       }
-      named_arrive(kBarFull + st, kPlainThreads);
+      named_arrive(kBarFull + st, NT);
       if (it + 1 < ntile) {
         nd = nd_next;
         if (it + 2 < ntile) nd_next = v.tiles[tile + 2 * gridDim.x].ndials;
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
     }
     // the reducers' last two EMPTY arrivals, so every named-barrier phase
     // gets its full count of threads
-    for (int j = ntile >= 2 ? ntile - 2 : 0; j < ntile; ++j) named_sync(kBarEmpty + (j & 1), kPlainThreads);
+    for (int j = ntile >= 2 ? ntile - 2 : 0; j < ntile; ++j) named_sync(kBarEmpty + (j & 1), NT);
     // after a failure, wait (bounded) for every copy still in flight before
     // the CTA's shared memory is released
     if (tid == 0 && s_fail) {
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
         s_bend[r] = 0;
       }
       named_sync(kBarRed, kWsRed);
-      named_sync(kBarFull + b, kPlainThreads);  // buffer b holds this tile's values
+      named_sync(kBarFull + b, NT);  // buffer b holds this tile's values
       const T* dv = dval + b * 1024;
       for (int e = r; e < td.nevents; e += kWsRed) {
         const uint16_t evi = sev[e];
@@ -354,7 +357,7 @@ __global__ void __launch_bounds__(kPlainThreads, sizeof(T) == 4 ? 3 : 2) k_plain
         if (e == 0 || ev_lbin(sev[e - 1]) != lb) s_bstart[lb] = e;
         if (e + 1 == td.nevents || ev_lbin(sev[e + 1]) != lb) s_bend[lb] = e + 1;
       }
-      named_arrive(kBarEmpty + b, kPlainThreads);  // buffer b consumed
+      named_arrive(kBarEmpty + b, NT);  // buffer b consumed
       named_sync(kBarRed, kWsRed);
       // one warp per local bin (two warps: bins w, w + 2): fixed-order FP64 sums
       for (int lb = rwarp; lb < (int)td.nbins; lb += 2) {
@@ -448,8 +451,8 @@ __global__ void __launch_bounds__(256) k_bins_llh(const DevView v, int K, double
 // ---------------------------------------------------------------------------
 size_t plain_smem_bytes(const DevView& v) {
   const size_t tsz = v.precision == 1 ? sizeof(float) : sizeof(double);
-  const size_t dv = (v.plain_kind == 1 ? 2048 : 1024) * tsz;
-  const size_t hb = v.plain_kind == 1 ? 2 * (size_t)v.tile_hdr_bytes : 0;
+  const size_t dv = (v.plain_kind >= 1 ? 2048 : 1024) * tsz;
+  const size_t hb = v.plain_kind >= 1 ? 2 * (size_t)v.tile_hdr_bytes : 0;
   return 2 * (size_t)v.tile_payload_bytes + hb + dv + kMaxTileEvents * sizeof(double) +
          kMaxTileEvents * sizeof(uint16_t);
 }
@@ -470,8 +473,13 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
 
 template <typename T>
 static const void* plain_fn(int kind) {
-  return kind == 1 ? (const void*)k_plain_ws<T> : (const void*)k_plain<T>;
+  if (kind == 2) return (const void*)k_plain_ws<T, 256>;
+  return kind == 1 ? (const void*)k_plain_ws<T, 192> : (const void*)k_plain<T>;
 }
+
+// threads of a K = 1 kernel kind (0: k_plain, 1: k_plain_ws with six
+// evaluator warps, 2: with eight)
+static int plain_threads(int kind) { return kind == 2 ? 256 + kWsRed : kind == 1 ? 192 + kWsRed : kPlainThreads; }
 
 // Every batched shape: the lanes-over-points family (gw_lanes.cu), the
 // dials-over-threads family (gw_multi.cu), then the warp-specialised small-K
@@ -520,7 +528,8 @@ int plain_blocks_per_sm(const DevView& v) {
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kPlainThreads, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, plain_threads(v.plain_kind), smem) != cudaSuccess)
+    return 0;
   return n;
 }
 
@@ -576,13 +585,22 @@ cudaError_t launch_table_fns(const DevView& v, int K, int max_size, cudaStream_t
 
 cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s) {
   const size_t smem = plain_smem_bytes(v);
-  if (v.plain_kind == 1) {
+  if (v.plain_kind == 2) {
+    const int nt = plain_threads(2);
     if (v.precision == 2)
-      k_plain_ws<dfloat><<<grid, kPlainThreads, smem, s>>>(v);
+      k_plain_ws<dfloat, 256><<<grid, nt, smem, s>>>(v);
     else if (v.precision)
-      k_plain_ws<float><<<grid, kPlainThreads, smem, s>>>(v);
+      k_plain_ws<float, 256><<<grid, nt, smem, s>>>(v);
     else
-      k_plain_ws<double><<<grid, kPlainThreads, smem, s>>>(v);
+      k_plain_ws<double, 256><<<grid, nt, smem, s>>>(v);
+  } else if (v.plain_kind == 1) {
+    const int nt = plain_threads(1);
+    if (v.precision == 2)
+      k_plain_ws<dfloat, 192><<<grid, nt, smem, s>>>(v);
+    else if (v.precision)
+      k_plain_ws<float, 192><<<grid, nt, smem, s>>>(v);
+    else
+      k_plain_ws<double, 192><<<grid, nt, smem, s>>>(v);
   } else {
     if (v.precision == 2)
       k_plain<dfloat><<<grid, kPlainThreads, smem, s>>>(v);

@@ -106,7 +106,8 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
         hw = max(hw, device_used_gb(torch) - base_used)
         r["plain_K1"] = {"ms_per_pass": ms1, "evals_per_s": 1e3 / ms1,
                          "hbm_gbs": bytes1 / (ms1 / 1e3) / 1e9, "frac": bytes1 / (ms1 / 1e3) / 1e9 / peak_bw,
-                         "algorithmic_bytes": bytes1, "kernel": ["k_plain", "k_plain_ws"][eng.plain_kernel()]}
+                         "algorithmic_bytes": bytes1,
+                         "kernel": ["k_plain", "k_plain_ws", "k_plain_ws (8 evaluator warps)"][eng.plain_kernel()]}
         eng.autotune(64)
         ms64 = time_eval(eng, torch, 64, p_dev, outs)
         hw = max(hw, device_used_gb(torch) - base_used)

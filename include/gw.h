@@ -274,8 +274,9 @@ int gw_set_shape(gw_engine* e, int32_t kind, int32_t points_per_pass, int32_t th
 
 /* The K = 1 kernel: 0 = one block pipeline per tile (k_plain), 1 =
  * warp-specialised (k_plain_ws: six warps evaluate the next tile's dials while
- * two form the current tile's products and bin partials).  gw_autotune(e, 1)
- * times both and keeps the faster.  Performance only: results are identical. */
+ * two form the current tile's products and bin partials), 2 = the same with
+ * eight evaluator warps.  gw_autotune(e, 1) times them and keeps the fastest.
+ * Performance only: results are identical. */
 int gw_set_plain_kernel(gw_engine* e, int32_t kind);
 int gw_get_plain_kernel(const gw_engine* e, int32_t* kind);
 

@@ -223,7 +223,7 @@ def test_autotune_picks_a_valid_shape(c1, c1_oracle):
     eng = Engine.from_workload(c1, precision="fp32", k_max=64)
     eng.autotune(64)
     kind, kc, th, st = eng.shape()
-    assert kind in (0, 1) and kc in (2, 4, 8, 16, 32, 64, 128) and th in (128, 256) and st in (1, 2)
+    assert kind in (0, 1, 3) and kc in (2, 4, 8, 16, 32, 64, 128) and th in (128, 256) and st in (1, 2)
     pts = c1.draw_points(64, 12)
     _check(eng.eval(pts), c1_oracle.eval(pts), FP32_BIN_REL, FP32_LLH_ABS)
     eng.close()
@@ -374,23 +374,24 @@ def test_engine_matches_reference_cache_manager_fixtures(name, cfg, events):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
-def test_both_k1_kernels_agree_bit_for_bit(mixed, prec):
-    """k_plain and the warp-specialised k_plain_ws form the same products and
-    sums in the same order: identical results, per-event weights included;
-    gw_autotune(1) picks one of them."""
+def test_all_k1_kernels_agree_bit_for_bit(mixed, prec):
+    """k_plain and the warp-specialised k_plain_ws (six or eight evaluator
+    warps) form the same products and sums in the same order: identical
+    results, per-event weights included; gw_autotune(1) picks one of them."""
     eng = Engine.from_workload(mixed, precision=prec, k_max=4)
     eng.set_event_weight_copy(True)
     pt = mixed.draw_points(1, 41)
     out = []
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         eng.set_plain_kernel(kind)
         assert eng.plain_kernel() == kind
         r = eng.eval(pt)
         out.append([np.array(x, copy=True) for x in r] + [eng.event_weights().copy()])
-    for x, y in zip(out[0], out[1]):
-        np.testing.assert_array_equal(x, y)
+    for other in out[1:]:
+        for x, y in zip(out[0], other):
+            np.testing.assert_array_equal(x, y)
     eng.autotune(1)
-    assert eng.plain_kernel() in (0, 1)
+    assert eng.plain_kernel() in (0, 1, 2)
     r = eng.eval(pt)
     np.testing.assert_array_equal(r[0], out[0][0])
     eng.close()
