@@ -959,7 +959,14 @@ int build_and_upload(gw_engine* e) {
             const int r = sorted[(size_t)i];
             evinfo[(size_t)i] = make_evinfo((int)ev_major.size(), e->bin[r] - tp.bin0);
             w0[(size_t)i] = (T)e->initial[r];
+            // an event's dials in type order (its product is formed in this
+            // order): consecutive dials of an event share a type, so kernels
+            // that evaluate two of them side by side rarely diverge
+            const size_t first = ev_major.size();
             for (int64_t j = rstart[r]; j < rstart[r + 1]; ++j) ev_major.push_back(byres[(size_t)j]);
+            std::stable_sort(ev_major.begin() + (std::ptrdiff_t)first, ev_major.end(), [&](int64_t a, int64_t b) {
+              return e->dials[(size_t)a].type < e->dials[(size_t)b].type;
+            });
           }
           const int nd = (int)ev_major.size();
           order.resize(nd);
