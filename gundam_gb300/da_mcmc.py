@@ -195,6 +195,9 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
     def stage1_of(su):
         if stage1 == "hmc":
             return mcmc.hmc_stage1(su.value_grad, L_post, eps=eps, n_leap=n_leap)
+        if stage1 == "hmc_base_grad":  # leapfrog on the base's gradient, acceptance on the full surrogate
+            return mcmc.hmc_stage1(su.value_grad, L_post, eps=eps, n_leap=n_leap,
+                                   guide=lin.value_grad if lin is not None and su is not lin else None)
         return lambda th, fs, ns, sd: su.substeps(th, fs, ns, sd)
     # both samplers start from the same states, taken after a delayed-
     # acceptance warm-up (it mixes fastest) so that neither starts out of
@@ -248,7 +251,8 @@ def run(events=0, train=65536, epochs=20, chains=64, steps=1000, n_sub=10, seed=
         "seconds_per_step": {"surrogate_substeps": t_sub, "surrogate_value_grad": t_grad, "exact": t_exact,
                              "points": chains},
         "stage1": {"kind": stage1, "n_sub": n_sub} if stage1 == "rwm" else
-                  {"kind": "hmc", "eps": eps, "n_leap": n_leap, "mass": "posterior covariance from the pilot"},
+                  {"kind": stage1, "eps": eps, "n_leap": n_leap, "mass": "posterior covariance from the pilot",
+                   "leapfrog_gradient": "the additive base's" if stage1 == "hmc_base_grad" else "the surrogate's"},
         "plain": dict(st_p, accept=p["accept"], n_exact=p["n_exact"]),
         "delayed": dict(st_d, stage2_accept=d["stage2_accept"], accept=d["accept"], n_exact=d["n_exact"],
                         n_surrogate=d["n_surrogate"], fell_back_at_step=d["fell_back_at_step"],
@@ -303,7 +307,7 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--thin", type=int, default=1)
     ap.add_argument("--warm-steps", type=int, default=500)
-    ap.add_argument("--stage1", default="hmc", choices=["hmc", "rwm"])
+    ap.add_argument("--stage1", default="hmc", choices=["hmc", "hmc_base_grad", "rwm"])
     ap.add_argument("--eps", type=float, default=0.25)
     ap.add_argument("--n-leap", type=int, default=10)
     ap.add_argument("--no-linear", action="store_true")

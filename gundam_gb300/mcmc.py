@@ -89,7 +89,7 @@ def adapt(f_exact, theta0, cov0, cycles=4, steps=150, seed=0, target=0.234, reco
             "chains": last if record_last else None}
 
 
-def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1):
+def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1, guide=None):
     """Stage 1 of delayed acceptance as Hamiltonian Monte Carlo on the
     surrogate density exp(-f_s/2): returns a callable (theta, fs, n, seed) ->
     (phi, f_s(phi), accepted) for ``delayed(stage1=...)``.
@@ -103,13 +103,23 @@ def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1):
     each transition is reversible with respect to exp(-f_s/2) and the
     delayed-acceptance correction keeps the exact posterior invariant.  The
     ``n`` argument of the callable is ignored in favour of ``n_trans`` except
-    that n == 0 only evaluates f_s."""
+    that n == 0 only evaluates f_s.
+
+    guide: another value_grad whose gradient drives the leapfrog steps (the
+    values at the trajectory's ends, and so the acceptance, stay f_s's).  A
+    smooth guide (the surrogate's additive base) keeps the trajectories from
+    following the network's rounding-level gradient noise; the map is still
+    volume-preserving and reversible, so the transition stays reversible with
+    respect to exp(-f_s/2)."""
     L = np.asarray(L, dtype=np.float64)
+    grad_of = guide if guide is not None else value_grad
 
     def stage1(theta, fs, n, seed):
         x = np.array(theta, dtype=np.float64)
         C, P = x.shape
         f, g = value_grad(x)
+        if guide is not None:
+            g = grad_of(x)[1]
         if n == 0:
             return x, f, np.zeros(C, np.int32)
         rng = np.random.default_rng(seed)
@@ -124,10 +134,12 @@ def hmc_stage1(value_grad, L, eps=0.25, n_leap=10, n_trans=1):
             fn, gn = f, g
             for step in range(n_leap):
                 xn = xn + e * (qn @ L.T)
-                fn, gn = value_grad(xn)
+                fn, gn = grad_of(xn)
                 if step + 1 < n_leap:
                     qn = qn - e * (0.5 * gn) @ L
             qn = qn - 0.5 * e * (0.5 * gn) @ L
+            if guide is not None:
+                fn = value_grad(xn)[0]
             h1 = 0.5 * fn + 0.5 * np.sum(qn * qn, axis=1)
             with np.errstate(over="ignore", invalid="ignore"):
                 a = np.log(np.maximum(u, 1e-300)) < (h0 - h1)

@@ -125,6 +125,34 @@ def test_delayed_with_hmc_stage1_is_exact_with_a_biased_surrogate():
     assert mcmc.ess(d["chains"], burn=60).min() > 5 * mcmc.ess(p["chains"], burn=60).min()
 
 
+def test_hmc_stage1_with_a_different_gradient_guide_is_exact():
+    """Leapfrog steps driven by another function's gradient (here a wrong,
+    smoother one), with the acceptance on the surrogate's own values: the
+    transition stays reversible with respect to the surrogate, and after the
+    stage-2 correction the chain samples the exact target."""
+    mean, cov, icov, f = _target()
+    shift = 0.2 * np.sqrt(np.diag(cov))
+    icov_s = np.linalg.inv(1.2 * cov)
+
+    def vg_sur(th):
+        d = th - mean - shift
+        return np.einsum("ij,jk,ik->i", d, icov_s, d), 2.0 * d @ icov_s
+
+    icov_g = np.linalg.inv(np.diag(np.diag(cov)) * 1.5)  # uncorrelated, too wide: a poor guide
+
+    def vg_guide(th):
+        d = th - mean
+        return np.einsum("ij,jk,ik->i", d, icov_g, d), 2.0 * d @ icov_g
+
+    Lc = np.linalg.cholesky(cov)
+    s1 = mcmc.hmc_stage1(vg_sur, Lc, eps=0.4, n_leap=6, guide=vg_guide)
+    r = mcmc.delayed(f, None, np.tile(mean, (32, 1)), 1500, Lc, n_sub=1, seed=7, max_error=1e9, stage1=s1)
+    x = r["chains"][200:].reshape(-1, mean.size)
+    assert np.allclose(x.mean(0), mean, atol=0.1)
+    assert np.allclose(x.std(0), np.sqrt(np.diag(cov)), rtol=0.1)
+    assert r["accept"] > 0.05
+
+
 def test_adaptive_pilot_learns_the_covariance_and_the_scale():
     """Started from a proposal 10x too wide and uncorrelated, the pilot's
     pooled covariance approaches the target's and its acceptance moves to
