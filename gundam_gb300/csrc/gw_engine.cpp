@@ -788,10 +788,16 @@ int build_and_upload(gw_engine* e) {
   const size_t tsz = sizeof(T);
   // stored form of Catmull-Rom splines (gw_config.flags; by default knot
   // values for FP32 K = 1 engines, precomputed slopes otherwise)
-  const int form = e->cfg.flags == GW_FLAG_SPLINE_KNOTS  ? kFormKnots
-                   : e->cfg.flags == GW_FLAG_SPLINE_COEFS ? kFormCoefs
-                   : (e->cfg.flags == 0 && e->cfg.k_max == 1 && tsz == 4) ? kFormKnots
-                                                                           : kFormSlopes;
+  // default: knot values for FP32 K = 1 engines (bandwidth-bound), the
+  // coefficient form for FP64 engines evaluating 16 or more points (their
+  // batched kernel is bound by the FP64 pipe: 92 ms against 124 ms for 64
+  // points of the 5M-event mixed workload), precomputed slopes otherwise
+  const int form = e->cfg.flags == GW_FLAG_SPLINE_KNOTS    ? kFormKnots
+                   : e->cfg.flags == GW_FLAG_SPLINE_COEFS   ? kFormCoefs
+                   : e->cfg.flags == GW_FLAG_SPLINE_SLOPES  ? kFormSlopes
+                   : (e->cfg.k_max == 1 && tsz == 4)        ? kFormKnots
+                   : (e->cfg.precision == GW_FP64 && e->cfg.k_max >= 16) ? kFormCoefs
+                                                                          : kFormSlopes;
 
   // 1. every result needs a bin (CacheManager.cpp:727-729 "Histogram cells are missing")
   for (int r = 0; r < N; ++r)
@@ -854,10 +860,12 @@ int build_and_upload(gw_engine* e) {
   }
 
   // 4. tiles
-  // default tile payload: 28 KB in FP32, 32 KB in FP64 (fastest of a 12-32 KB
-  // sweep on the 5M-event mixed workload at K = 1 and K = 64; larger FP32 tiles
-  // cost the K = 1 kernel its third CTA per SM)
-  const int64_t tile_default = tsz == 4 ? 28672 : 32768;
+  // default tile payload: 28 KB in FP32 (fastest of a 12-32 KB sweep on the
+  // 5M-event mixed workload at K = 1 and K = 64; larger FP32 tiles cost the
+  // K = 1 kernel its third CTA per SM), 40 KB for the 8-byte precisions (FP64
+  // and double-float: fastest of 16-48 KB at K = 1 and K = 64; at 48 KB one
+  // CTA per SM is left)
+  const int64_t tile_default = tsz == 4 ? 28672 : 40960;
   int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : tile_default) / (int64_t)tsz;
   cap_elems = std::min<int64_t>(cap_elems, kMaxPayloadElems);
   cap_elems = std::max<int64_t>(cap_elems, 64);
@@ -959,14 +967,7 @@ int build_and_upload(gw_engine* e) {
             const int r = sorted[(size_t)i];
             evinfo[(size_t)i] = make_evinfo((int)ev_major.size(), e->bin[r] - tp.bin0);
             w0[(size_t)i] = (T)e->initial[r];
-            // an event's dials in type order (its product is formed in this
-            // order): consecutive dials of an event share a type, so kernels
-            // that evaluate two of them side by side rarely diverge
-            const size_t first = ev_major.size();
             for (int64_t j = rstart[r]; j < rstart[r + 1]; ++j) ev_major.push_back(byres[(size_t)j]);
-            std::stable_sort(ev_major.begin() + (std::ptrdiff_t)first, ev_major.end(), [&](int64_t a, int64_t b) {
-              return e->dials[(size_t)a].type < e->dials[(size_t)b].type;
-            });
           }
           const int nd = (int)ev_major.size();
           order.resize(nd);

@@ -78,8 +78,6 @@ cudaError_t launch_plain(const DevView& v, int grid, cudaStream_t s);
 // kc points per warp pass, kr points per lane.  kind 1 = k_multi: threads over
 // dials, kc points per chunk, kr points per thread.  kind 3 = k_ws: the
 // warp-specialised K = 1 kernel with kc = kr points per evaluator thread.
-// kind 4 = k_pairs: lanes over points, two dials per warp step, kc = 64
-// points per pass, kr = 4 points per lane.
 // threads per block and
 // payload stages for both; minb = CTAs per SM the kernel's register
 // allocation targets (its launch bounds; 0 = the compiler's choice).
@@ -102,9 +100,6 @@ int multi_shapes(const ShapeEntry** out);  // gw_multi.cu
 // kind 3 = k_ws (gw_ws.cu): the warp-specialised K = 1 kernel with kc points
 // per evaluator thread (kr = kc).
 int ws_shapes(const ShapeEntry** out);
-// kind 4 = k_pairs (gw_lanes.cu): the two half-warps evaluate two dials of an
-// event side by side, 16 lanes x 4 points = 64 points per pass (kc = 64, kr = 4).
-int pair_shapes(const ShapeEntry** out);
 size_t ws_smem_bytes(const DevView& v, int kc);
 cudaError_t launch_batched(const DevView& v, int K, const BatchedShape& b, int grid, cudaStream_t s);
 // True when every pass of the shape over K points stays inside the kpad

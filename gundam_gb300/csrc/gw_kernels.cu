@@ -482,27 +482,24 @@ static const void* plain_fn(int kind) {
 static int plain_threads(int kind) { return kind == 2 ? 256 + kWsRed : kind == 1 ? 192 + kWsRed : kPlainThreads; }
 
 // Every batched shape: the lanes-over-points family (gw_lanes.cu), the
-// dials-over-threads family (gw_multi.cu), the warp-specialised small-K
-// family (gw_ws.cu), then the dial-pairs family (gw_lanes.cu).
+// dials-over-threads family (gw_multi.cu), then the warp-specialised small-K
+// family (gw_ws.cu).
 static const ShapeEntry* shape_entry(int i) {
   const ShapeEntry* lanes;
   const ShapeEntry* multi;
   const ShapeEntry* ws;
-  const ShapeEntry* pairs;
   const int nl = lane_shapes(&lanes);
   const int nm = multi_shapes(&multi);
   const int ns = ws_shapes(&ws);
-  const int np = pair_shapes(&pairs);
-  if (i < 0 || i >= nl + nm + ns + np) return nullptr;
+  if (i < 0 || i >= nl + nm + ns) return nullptr;
   if (i < nl) return &lanes[i];
   if (i < nl + nm) return &multi[i - nl];
-  if (i < nl + nm + ns) return &ws[i - nl - nm];
-  return &pairs[i - nl - nm - ns];
+  return &ws[i - nl - nm];
 }
 
 int batched_shape_count() {
   const ShapeEntry* p;
-  return lane_shapes(&p) + multi_shapes(&p) + ws_shapes(&p) + pair_shapes(&p);
+  return lane_shapes(&p) + multi_shapes(&p) + ws_shapes(&p);
 }
 
 BatchedShape batched_shape(int i) {

@@ -174,179 +174,6 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// K > 1, dial pairs: the two half-warps evaluate two consecutive dials of the
-// same event side by side, each lane at KR = 4 points (16 lanes x 4 = 64
-// points per pass), so a dial's header decode, type dispatch, parameter and
-// clamp loads are paid once per 4 points instead of 2.  An event's dials are
-// stored in type order, so the two dials of a pair mostly share a type (the
-// half-warps then run one code path).  The half products are combined by one
-// shuffle per point and the lower half-warp accumulates the FP64 partials;
-// the tile pipeline and the partial-sum layout are k_batched's with KC = 16,
-// KR = 4.
-// ---------------------------------------------------------------------------
-template <typename T, int NT, int ST, int MB>
-__global__ void __launch_bounds__(NT, MB) k_pairs(const DevView v, int K) {
-  constexpr int KC = 16, KR = 4;
-  constexpr int NW = NT / 32;
-  constexpr int KP = KC * KR;  // 64 points per pass
-  constexpr int NE = NW + kMaxLocalBins - 1;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int TB = v.tile_payload_bytes;
-  unsigned char* stage0 = smem;
-  unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
-  uint64_t* shdr = (uint64_t*)(smem + ST * TB);               // [1024], indexed by slot
-  double2* wpart = (double2*)(shdr + 1024);                   // [NE][KR][32] (lanes 0..15 used)
-  T* sw0 = (T*)(wpart + NE * KR * 32);                        // [256]
-  uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
-  __shared__ uint64_t bar[2];
-  __shared__ int s_present[kMaxLocalBins];
-  __shared__ int s_run[NW][2];
-
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int half = lane >> 4, kl = lane & 15;
-  if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-
-  int tile = blockIdx.x;
-  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
-  for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
-    const int st = (ST == 2) ? (it & 1) : 0;
-    const uint32_t parity = (ST == 2) ? (uint32_t)((it >> 1) & 1) : (uint32_t)(it & 1);
-    const int next = tile + gridDim.x;
-    if (ST == 2 && tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
-
-    const TileDesc td = v.tiles[tile];
-    const int nd = td.ndials, ne = td.nevents;
-    for (int i = tid; i < nd; i += NT) {
-      const uint64_t h = v.hdr[td.dial0 + i];
-      shdr[hdr_slot(h)] = h;
-    }
-    for (int e = tid; e < ne; e += NT) {
-      sev[e] = v.evinfo[td.event0 + e];
-      sw0[e] = ((const T*)v.w0)[td.event0 + e];
-    }
-    if (tid == 0) sev[ne] = make_evinfo(nd, 0);
-    if (tid < kMaxLocalBins) s_present[tid] = 0;
-    const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) {
-        atomicOr(v.status, kStatusCopyTimeout);
-        if (ST == 2 && next < v.n_tiles)
-          mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
-      }
-      return;
-    }
-    for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
-    const T* pl = (const T*)(st ? stage1 : stage0);
-
-    auto first_event_at = [&](int target) {
-      int lo = 0, hi = ne;  // sev[ne] holds nd
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (ev_slot(sev[mid]) < target) lo = mid + 1;
-        else hi = mid;
-      }
-      return lo;
-    };
-    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * nd) / NW);
-    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * nd) / NW);
-    const int b_first = (e_lo < e_hi) ? ev_lbin(sev[e_lo]) : 1;
-    const int b_last = (e_lo < e_hi) ? ev_lbin(sev[e_hi - 1]) : 0;
-    if (lane == 0) {
-      s_run[warp][0] = b_first;
-      s_run[warp][1] = b_last;
-    }
-
-    for (int kb = 0; kb < K; kb += KP) {
-      const int k0 = kb + kl;  // this lane's points: k0 + j*KC
-      for (int lb = b_first; lb <= b_last; ++lb)
-#pragma unroll
-        for (int j = 0; j < KR; ++j) wpart[((warp + lb) * KR + j) * 32 + lane] = make_double2(0.0, 0.0);
-      int cur = -1;
-      double s[KR], s2[KR];
-#pragma unroll
-      for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
-      for (int e = e_lo; e < e_hi; ++e) {
-        const uint16_t ei = sev[e];
-        const int s0 = ev_slot(ei), s1 = ev_slot(sev[e + 1]);
-        T w[KR];
-#pragma unroll
-        for (int j = 0; j < KR; ++j) w[j] = T(1);
-        for (int sl = s0 + half; sl < s1; sl += 2) {
-          T val[KR];
-          dial_values<T, KR>(v, shdr[sl], pl, k0, KC, val);
-#pragma unroll
-          for (int j = 0; j < KR; ++j) w[j] *= val[j];
-        }
-        // the other half-warp's product of the same points
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          if constexpr (kIsDf<T>) {
-            const dfloat o(__shfl_xor_sync(0xffffffffu, w[j].hi, 16), __shfl_xor_sync(0xffffffffu, w[j].lo, 16));
-            w[j] *= o;
-          } else {
-            w[j] *= __shfl_xor_sync(0xffffffffu, w[j], 16);
-          }
-        }
-        const T w0 = sw0[e];
-        const int lb = ev_lbin(ei);
-        if (lb != cur) {
-          if (cur >= 0 && half == 0) {
-#pragma unroll
-            for (int j = 0; j < KR; ++j) wpart[((warp + cur) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
-          }
-          cur = lb;
-#pragma unroll
-          for (int j = 0; j < KR; ++j) s[j] = s2[j] = 0.0;
-        }
-#pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          T wj = w[j];
-          if (v.has_cap && wj > (T)v.cap) wj = (T)v.cap;
-          wj = w0 * wj;
-          const double wd = (double)wj;
-          s[j] += wd;
-          s2[j] += wd * wd;
-        }
-      }
-      if (cur >= 0 && half == 0) {
-#pragma unroll
-        for (int j = 0; j < KR; ++j) wpart[((warp + cur) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
-      }
-      __syncthreads();
-      for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
-        const int lb = t / KP, r = t % KP;
-        const int j = r / KC, kk = r % KC;
-        const int kg = kb + kk + j * KC;
-        if (kg < K && lb < (int)td.nbins && s_present[lb]) {
-          double a = 0.0, a2 = 0.0;
-          for (int w = 0; w < NW; ++w) {
-            if (lb < s_run[w][0] || lb > s_run[w][1]) continue;
-            const double2 p = wpart[((w + lb) * KR + j) * 32 + kk];
-            a += p.x;
-            a2 += p.y;
-          }
-          const int slot = (lb == 0) ? (int)td.slot0 : v.bin_slot[td.bin0 + lb];
-          v.partials[(size_t)slot * v.kpad + kg] = make_double2(a, a2);
-        }
-      }
-      __syncthreads();
-    }
-    if (ST == 1 && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
-  }
-}
-
-template <typename T, int NT, int ST, int MB>
-void launch_p(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
-  k_pairs<T, NT, ST, MB><<<grid, NT, smem, s>>>(v, K);
-}
-
 template <typename T, int KC, int KR, int NT, int ST, int MB>
 void launch_b(const DevView& v, int K, int grid, size_t smem, cudaStream_t s) {
   k_batched<T, KC, KR, NT, ST, MB><<<grid, NT, smem, s>>>(v, K);
@@ -379,25 +206,11 @@ const ShapeEntry kLaneShapes[] = {
 #undef GW_SHAPE2
 #undef GW_SHAPE
 
-// family 4 (k_pairs): 64 points per pass (16 lanes x 4 points), FP32 only
-#define GW_PAIRS(NT, ST, MB)                                                                       \
-  {4, 64, 4, NT, ST, MB, {nullptr, (const void*)k_pairs<float, NT, ST, MB>, nullptr},             \
-   {nullptr, launch_p<float, NT, ST, MB>, nullptr}}
-const ShapeEntry kPairShapes[] = {
-    GW_PAIRS(256, 1, 0), GW_PAIRS(256, 1, 2), GW_PAIRS(256, 1, 3), GW_PAIRS(256, 2, 2),
-};
-#undef GW_PAIRS
-
 }  // namespace
 
 int lane_shapes(const ShapeEntry** out) {
   *out = kLaneShapes;
   return (int)(sizeof(kLaneShapes) / sizeof(kLaneShapes[0]));
-}
-
-int pair_shapes(const ShapeEntry** out) {
-  *out = kPairShapes;
-  return (int)(sizeof(kPairShapes) / sizeof(kPairShapes[0]));
 }
 
 }  // namespace gw

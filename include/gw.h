@@ -73,10 +73,11 @@ enum {
  * splines.  Knot values only, [low, 1/step, y x n], the reference's own data,
  * with the knot slopes formed in the kernel (fewer bytes per evaluation); or
  * with the slopes precomputed on the host, [low, 1/step, (y, slope) x n]
- * (less arithmetic per evaluation).  Neither flag: knot values for FP32
- * engines with k_max == 1 (a bandwidth-bound evaluation), precomputed slopes
- * otherwise (batched evaluation, and FP64, which GB300's FP64 rate makes
- * arithmetic-bound).  Results agree within the precision's rounding; in FP64
+ * (less arithmetic per evaluation).  No flag: knot values for FP32 engines
+ * with k_max == 1 (a bandwidth-bound evaluation), the coefficient form below
+ * for FP64 engines with k_max >= 16 (GB300's FP64 rate makes their batched
+ * evaluation arithmetic-bound), precomputed slopes otherwise.  Results agree
+ * within the precision's rounding; in FP64
  * the per-event weights are identical (the bin sums then differ only in the
  * grouping of their FP64 partial sums, as the tiles are cut differently). */
 enum {
@@ -119,7 +120,7 @@ typedef struct gw_config {
   int32_t k_max;      /* largest number of parameter points per gw_eval (>= 1) */
   int32_t precision;  /* GW_FP64, GW_FP32 or GW_DF64 */
   int32_t device;     /* CUDA device ordinal */
-  int32_t tile_bytes; /* payload bytes per tile; 0 = default (28672 FP32, 32768 FP64) */
+  int32_t tile_bytes; /* payload bytes per tile; 0 = default (28672 FP32, 40960 FP64 and double-float) */
   int32_t flags;      /* 0 or one GW_FLAG_SPLINE_* value */
 } gw_config;
 

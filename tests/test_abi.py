@@ -164,9 +164,7 @@ def test_compiled_shape_list():
     shapes = Engine.compiled_shapes()
     assert len(shapes) >= 10
     for kind, ppp, ppt, threads, stages, minb in shapes:
-        assert kind in (0, 1, 3, 4) and threads in (128, 256) and stages in (1, 2) and minb >= 0
-        if kind == 4:  # dial pairs: 16 lanes x 4 points per half-warp
-            assert ppp == 64 and ppt == 4
+        assert kind in (0, 1, 3) and threads in (128, 256) and stages in (1, 2) and minb >= 0
         if kind == 3:  # small-K warp-specialised: every evaluator thread takes all points of a pass
             assert ppp == ppt and ppp % 2 == 0 and threads == 256
         if kind == 0:
