@@ -499,34 +499,30 @@ def run_gw(args, world, rank, local, dist):
             variants[f"{args.precision}_K16"] = {"evals_per_s": 16e3 / ms16, "ms_per_step": ms16, "kernel_ms": kms16,
                                                   "shape": list(eng.shape())}
         if args.precision == "fp32":
-            eng.close()
-            eng = Engine.from_workload(wl, precision="fp64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
-                                       device=local)
-            eng.autotune(1)
-            ms64, kms64, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-            variants["fp64_K1"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
-                "evals_per_s": 1e3 / ms64, "ms_per_eval": ms64, "kernel_ms": kms64,
-                "kernel_gbs": algorithmic_bytes(wl, "fp64", 1) / (kms64 / 1e3) / 1e9}
-            if K > 1:
-                eng.autotune(K)
-                msk, kmsk, _ = time_device(eng, torch, d, K, min(args.steps, 20), args.warmup, dist)
-                variants[f"fp64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk}
-            # the same in double-float (two FP32 words per value on the FP32
-            # pipe, sums and LLH in FP64; held to the FP64 parity bar)
-            eng.close()
-            eng = Engine.from_workload(wl, precision="df64", k_max=max(K, 1), llh_type=llh_type_for(args.config),
-                                       device=local)
-            eng.autotune(1)
-            msd, kmsd, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-            algd = algorithmic_bytes(wl, "df64", 1)
-            variants["df64_K1"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
-                "evals_per_s": 1e3 / msd, "ms_per_eval": msd, "kernel_ms": kmsd,
-                "kernel_gbs": algd / (kmsd / 1e3) / 1e9, "kernel_frac_of_hbm_peak": algd / (kmsd / 1e3) / 1e9 / peak}
-            if K > 1:
-                eng.autotune(K)
-                msk, kmsk, _ = time_device(eng, torch, d, K, min(args.steps, 20), args.warmup, dist)
-                variants[f"df64_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk,
-                                          "shape": list(Engine.compiled_shapes()[eng.shape_index()])}
+            # the reference's precision (FP64) and the double-float mode (two
+            # FP32 words per value on the FP32 pipe, sums and LLH in FP64, held
+            # to the FP64 parity bar): K = 1 on a K = 1 engine, K points on an
+            # engine sized for them, each with its default spline form
+            for prec in ("fp64", "df64"):
+                eng.close()
+                eng = Engine.from_workload(wl, precision=prec, k_max=1, llh_type=llh_type_for(args.config),
+                                           device=local)
+                eng.autotune(1)
+                ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
+                alg1 = algorithmic_bytes(wl, prec, 1)
+                variants[f"{prec}_K1"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
+                    "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
+                    "kernel_gbs": alg1 / (kms1 / 1e3) / 1e9, "kernel_frac_of_hbm_peak": alg1 / (kms1 / 1e3) / 1e9 / peak,
+                    "payload_bytes": eng.layout()["payload_bytes"]}
+                if K > 1:
+                    eng.close()
+                    eng = Engine.from_workload(wl, precision=prec, k_max=K, llh_type=llh_type_for(args.config),
+                                               device=local)
+                    eng.autotune(K)
+                    msk, kmsk, _ = time_device(eng, torch, d, K, min(args.steps, 20), args.warmup, dist)
+                    variants[f"{prec}_K{K}"] = {"evals_per_s": K * 1e3 / msk, "ms_per_step": msk, "kernel_ms": kmsk,
+                                                "shape": list(Engine.compiled_shapes()[eng.shape_index()]),
+                                                "payload_bytes": eng.layout()["payload_bytes"]}
             if K < 256:
                 eng.close()
                 K2 = 256
