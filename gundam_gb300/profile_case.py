@@ -1,13 +1,14 @@
 """A small, self-contained case for profiling one kernel under ncu.
 
-    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64} [n_events] [shape_index] [K]
+    python -m gundam_gb300.profile_case {plain|batched} {fp32|fp64|df64} [n_events] [shape_index] [K]
     python -m gundam_gb300.profile_case train [steps]
     python -m gundam_gb300.profile_case substeps [n_sub]
 
 plain / batched: builds the C2-shaped workload with n_events events (default
 1,000,000: a payload above the 129 MB L2 but a few GB of device memory at
-most) and evaluates it four times: K = 1 (the K = 1 kernel, on a K = 1
-engine: Catmull-Rom splines stored as knot values in FP32) or K points
+most) and evaluates it four times: K = 1 (the K = 1 kernel the autotuner
+picks, on a K = 1 engine: Catmull-Rom splines stored as knot values in FP32;
+the autotuner's launches come before the four) or K points
 (default 64) with batched shape `shape_index` (an entry of
 Engine.compiled_shapes(); -1 or none: the autotuner picks one first, and the
 chosen index is printed).
@@ -75,10 +76,13 @@ def main(argv):
             eng.set_shape_index(int(argv[3]))
         else:
             eng.autotune(K)
+    else:
+        eng.autotune(1)  # the K = 1 kernel kind the engine would pick
     pts = wl.draw_points(K, 5)
     for _ in range(4):
         eng.eval(pts)
-    print("ok", eng.layout()["payload_bytes"], eng.shape(), "shape index", eng.shape_index())
+    print("ok", eng.layout()["payload_bytes"], eng.shape(), "shape index", eng.shape_index(),
+          "K = 1 kernel", eng.plain_kernel())
 
 
 if __name__ == "__main__":
