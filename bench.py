@@ -236,6 +236,55 @@ def time_device(eng, torch, d, K, steps, warmup, dist):
     return ms, kms / max(1, klaunch), launches
 
 
+def cpu_baseline_checks(c1_check, c3_check, c5_check, threads=None):
+    """The CPU-baseline leg's second task: the CPU propagation (FP64) of the
+    same parameter points the engine evaluated for C1, C3 and C5, timed, and
+    the engine's per-bin and LLH errors against it."""
+    from gundam_gb300 import Workload
+    from oracle.oracle import Oracle
+
+    threads = threads or (os.cpu_count() or 1)
+    res = {}
+    if c1_check is not None or c3_check is not None:
+        wl = Workload("c1", seed=2)
+        orc = Oracle(wl, llh_type=llh_type_for("c1"))
+        if c1_check is not None:
+            t0 = time.perf_counter()
+            ref = orc.eval(c1_check["points"], threads=threads)
+            dt = time.perf_counter() - t0
+            res["c1"] = {"cpu_evals_per_s": len(c1_check["points"]) / dt, "cpu_threads": threads}
+            for key, (sums, llh) in c1_check["outputs"].items():
+                res["c1"][key] = errors_vs_oracle(sums, llh, ref)
+        if c3_check is not None:
+            res["c3"] = {}
+            for key, pts in c3_check["points"].items():
+                sums, llh = c3_check["outputs"][key]
+                res["c3"][key] = errors_vs_oracle(sums, llh, orc.eval(pts, threads=threads))
+        orc.close()
+        wl.close()
+    if c5_check is not None:
+        from gundam_gb300.stress import host_available_gb
+
+        need = 1.6 * c5_check["events"] / 1e6  # GB: the workload (~60 GB at 40M events) and the CPU path's arrays
+        if host_available_gb() < need:
+            res["c5"] = {"skipped": f"host has {host_available_gb():.0f} GB available, the check needs ~{need:.0f} GB"}
+            return res
+        # the 40M-event workload again (the GPU run released its copy)
+        wl = Workload("c5", n_events=c5_check["events"], seed=c5_check["seed"])
+        orc = Oracle(wl, llh_type=llh_type_for("c5"))
+        t0 = time.perf_counter()
+        ref = orc.eval(c5_check["points"], threads=threads)
+        dt = time.perf_counter() - t0
+        res["c5"] = {"cpu_evals_per_s": len(c5_check["points"]) / dt, "cpu_threads": threads,
+                     "points": len(c5_check["points"])}
+        for key, (sums, llh) in c5_check["outputs"].items():
+            k = len(llh)
+            res["c5"][key] = errors_vs_oracle(sums, llh, {"sums": ref["sums"][:k], "llh": ref["llh"][:k]})
+        orc.close()
+        wl.close()
+    return res
+
+
 def errors_vs_oracle(sums, llh, ref):
     """Largest per-bin relative error of the bin sums (bins the oracle leaves
     empty must be 0 exactly) and largest absolute LLH error."""
@@ -253,23 +302,20 @@ def c1_points(local, n_points=1000):
     """C1 (100k events, Poisson LLH, 20 parameters): bin contents and LLH at
     1000 random parameter points from the prior, FP64 engine (the plain K = 1
     kernel point by point, and all 1000 in batched launches of 250) and FP32
-    dials, each against the FP64 oracle on the same points; rates through
-    gw_eval with host buffers."""
+    dials; rates through gw_eval with host buffers.  Returns the record and
+    the engine outputs, which the CPU-baseline leg checks against the CPU
+    propagation of the same points."""
+    import numpy as np
+
     from gundam_gb300 import Engine, Workload
-    from oracle.oracle import Oracle
 
     wl = Workload("c1", seed=2)
     pts = wl.draw_points(n_points, 2024)
-    t0 = time.perf_counter()
-    orc = Oracle(wl, llh_type=llh_type_for("c1"))
-    ref = orc.eval(pts)
-    orc.close()
     out = {"workload": f"c1: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
-           "points": n_points, "oracle_seconds": time.perf_counter() - t0,
+           "points": n_points,
            "tolerance": {"fp64": "per-bin relative 1e-12, LLH absolute 1e-6",
                          "fp32": "per-bin relative 2e-5, LLH absolute 5e-2"}}
-    import numpy as np
-
+    outputs = {}
     for prec, K in (("fp64", 1), ("fp64", 250), ("fp32", 250)):
         eng = Engine.from_workload(wl, precision=prec, k_max=K, llh_type=llh_type_for("c1"), device=local)
         eng.autotune(K)
@@ -281,10 +327,11 @@ def c1_points(local, n_points=1000):
             s_, _, l_, _ = eng.eval(pts[a:a + K])
             sums[a:a + K], llh[a:a + K] = s_, l_
         dt = time.perf_counter() - t0
-        out[f"{prec}_K{K}"] = dict(errors_vs_oracle(sums, llh, ref), evals_per_s=n_points / dt,
-                                   launches_of_points=K)
+        out[f"{prec}_K{K}"] = {"evals_per_s": n_points / dt, "launches_of_points": K}
+        outputs[f"{prec}_K{K}"] = (sums, llh)
         eng.close()
-    return out
+    wl.close()
+    return out, {"config": "c1", "points": pts, "outputs": outputs}
 
 
 def c3_sweep(local, steps=20, warmup=3):
@@ -295,11 +342,11 @@ def c3_sweep(local, steps=20, warmup=3):
     import torch
 
     from gundam_gb300 import Engine, Workload
-    from oracle.oracle import Oracle
 
     wl = Workload("c1", seed=2)
     out = {"workload": f"c1: {wl.n_events} events, {wl.n_dials} dials, {wl.n_bins} bins, {wl.n_params} params",
            "note": "the C1 payload (~10 MB) is L2-resident"}
+    check = {"config": "c1", "points": {}, "outputs": {}}
     for K in (16, 64, 256):
         eng = Engine.from_workload(wl, precision="fp32", k_max=K, llh_type=llh_type_for("c1"), device=local)
         eng.autotune(K)
@@ -320,15 +367,14 @@ def c3_sweep(local, steps=20, warmup=3):
         b.record(stream)
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / steps
-        sh, lh = s.cpu().numpy(), ll.cpu().numpy()
         eng.sync()
-        orc = Oracle(wl, llh_type=llh_type_for("c1"))
-        err = errors_vs_oracle(sh, lh, orc.eval(pts.cpu().numpy()))
-        orc.close()
-        out[f"K{K}"] = dict({"evals_per_s": K * 1e3 / ms, "ms_per_launch": ms, "shape": list(eng.shape())}, **err)
+        out[f"K{K}"] = {"evals_per_s": K * 1e3 / ms, "ms_per_launch": ms, "shape": list(eng.shape())}
+        check["points"][f"K{K}"] = pts.cpu().numpy()
+        check["outputs"][f"K{K}"] = (s.cpu().numpy(), ll.cpu().numpy())
         eng.close()
-    out["error_against"] = "the FP64 oracle on the same K points (FP32 dials, FP64 sums and LLH)"
-    return out
+    wl.close()
+    out["error_against"] = "the CPU propagation (FP64) of the same K points (FP32 dials, FP64 sums and LLH)"
+    return out, check
 
 
 def mcmc_comparison(args):
@@ -553,13 +599,28 @@ def run_gw(args, world, rank, local, dist):
             if "e2e_evals_per_s" in var:
                 var["e2e_over_cpu_baseline"] = var["e2e_evals_per_s"] / cpu["value"]
     c3 = c1 = c5 = None
+    c1_check = c3_check = c5_check = None
     if rank == 0 and not args.no_variants:
-        c3 = c3_sweep(local)
-        c1 = c1_points(local)
+        c3, c3_check = c3_sweep(local)
+        c1, c1_check = c1_points(local)
     if rank == 0 and not args.no_c5 and args.config == "c2":
         from gundam_gb300 import stress
 
-        c5 = stress.run()
+        c5 = stress.run(check_points=2)
+        c5_check = c5.pop("check", None)
+    if rank == 0 and (c1_check or c3_check or c5_check):
+        chk = cpu_baseline_checks(c1_check, c3_check, c5_check)
+        if c1 is not None and "c1" in chk:
+            for key, v in chk["c1"].items():
+                if isinstance(v, dict):
+                    c1[key].update(v)
+                else:
+                    c1[key] = v
+        if c3 is not None and "c3" in chk:
+            for key, v in chk["c3"].items():
+                c3[key].update(v)
+        if c5 is not None and "c5" in chk:
+            c5["parity_against_cpu_propagation"] = chk["c5"]
     mc = None
     if rank == 0 and not args.no_mcmc and args.config == "c2":
         mc = mcmc_comparison(args)

@@ -64,7 +64,12 @@ def time_eval(eng, torch, K, pts_dev, outs, steps=5, warmup=2):
     return a.elapsed_time(b) / steps
 
 
-def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
+def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print, check_points=0):
+    """check_points > 0: the engine's bin sums and likelihood at the first
+    check_points parameter points (the K = 1 kernel at the first one, the
+    K = 64 batched shape at all of them) are returned under "check", with the
+    points and the workload's size and seed, for a comparison with the CPU
+    propagation of the same workload."""
     import torch
 
     peak_bw = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"] \
@@ -74,6 +79,7 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
     if avail == avail and avail < need:
         return {"skipped": f"host has {avail:.0f} GB available, the build needs ~{need:.0f} GB"}
     out = {"events": events, "host_available_gb": avail, "peak_hbm_gbs": peak_bw}
+    check = {"events": events, "seed": seed, "outputs": {}} if check_points > 0 else None
     torch.cuda.init()
     base_used = device_used_gb(torch)
     for prec in precisions:
@@ -86,6 +92,8 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
         bytes1 = algorithmic_bytes(wl, prec, 1)
         bytes64 = algorithmic_bytes(wl, prec, 64)
         pts = wl.draw_points(64, 11)
+        if check is not None:
+            check["points"] = pts[:check_points]
         t0 = time.perf_counter()
         eng = Engine.from_workload(wl, precision=prec, k_max=64, initialize=False)
         r["cache_build_s"] = time.perf_counter() - t0
@@ -103,6 +111,9 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
                 torch.empty(64, dtype=torch.float64, device="cuda"))
         eng.autotune(1)
         ms1 = time_eval(eng, torch, 1, p_dev, outs)
+        if check is not None:
+            s1, _, l1, _ = eng.eval(pts[:1])
+            check["outputs"][f"{prec}_K1"] = (s1.copy(), l1.copy())
         hw = max(hw, device_used_gb(torch) - base_used)
         r["plain_K1"] = {"ms_per_pass": ms1, "evals_per_s": 1e3 / ms1,
                          "hbm_gbs": bytes1 / (ms1 / 1e3) / 1e9, "frac": bytes1 / (ms1 / 1e3) / 1e9 / peak_bw,
@@ -110,6 +121,9 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
                          "kernel": ["k_plain", "k_plain_ws", "k_plain_ws (8 evaluator warps)"][eng.plain_kernel()]}
         eng.autotune(64)
         ms64 = time_eval(eng, torch, 64, p_dev, outs)
+        if check is not None:
+            sk, _, lk, _ = eng.eval(pts[:check_points])
+            check["outputs"][f"{prec}_batched"] = (sk.copy(), lk.copy())
         hw = max(hw, device_used_gb(torch) - base_used)
         r["batched_K64"] = {"ms_per_pass": ms64, "evals_per_s": 64e3 / ms64,
                             "hbm_gbs": bytes64 / (ms64 / 1e3) / 1e9, "shape": list(eng.shape()),
@@ -123,6 +137,8 @@ def run(events=40_000_000, precisions=("fp32", "fp64"), seed=2, log=print):
         del eng, p_dev, outs
         gc.collect()
         torch.cuda.empty_cache()
+    if check is not None:
+        out["check"] = check
     return out
 
 
