@@ -227,17 +227,22 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       // clamps are one clamp to the intersection.
       if (lo < T(-1e20)) lo = T(-1e20);
       if (hi > T(1e20)) hi = T(1e20);
-      if (v.spline_coefs && (type == kMonotonic || type == kUniform || type == kCompact)) {
-        coef_values<T, KR>(d, n, x, trunc, val);
-      } else if (type == kMonotonic) {
-        if (v.spline_knots) {
+      // the stored spline form is checked inside each spline type's branch,
+      // so the other types pay nothing for it
+      if (type == kMonotonic) {
+        if (v.spline_coefs) {
+          coef_values<T, KR>(d, n, x, trunc, val);
+        } else if (v.spline_knots) {
 #pragma unroll
           for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, true>(d, n, x[j], trunc);
         } else {
           prepared_values<T, true, KR>(d, n, x, trunc, val);
         }
       } else if (type == kUniform) {
-        prepared_values<T, false, KR>(d, n, x, trunc, val);
+        if (v.spline_coefs)
+          coef_values<T, KR>(d, n, x, trunc, val);
+        else
+          prepared_values<T, false, KR>(d, n, x, trunc, val);
       } else if (type == kGeneral) {
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_general<T>(d, n, x[j], trunc);
@@ -250,7 +255,9 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
 #pragma unroll
         for (int j = 0; j < KR; ++j) val[j] = eval_bilinear<T>(d, x[j], y[j], trunc);
       } else if (type == kCompact) {
-        if (v.spline_knots) {
+        if (v.spline_coefs) {
+          coef_values<T, KR>(d, n, x, trunc, val);
+        } else if (v.spline_knots) {
 #pragma unroll
           for (int j = 0; j < KR; ++j) val[j] = eval_knots<T, false>(d, n, x[j], trunc);
         } else {

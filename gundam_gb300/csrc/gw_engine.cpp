@@ -861,11 +861,13 @@ int build_and_upload(gw_engine* e) {
 
   // 4. tiles
   // default tile payload: 28 KB in FP32 (fastest of a 12-32 KB sweep on the
-  // 5M-event mixed workload at K = 1 and K = 64; larger FP32 tiles cost the
-  // K = 1 kernel its third CTA per SM), 40 KB for the 8-byte precisions (FP64
+  // 5M-event mixed workload at K = 1; larger FP32 tiles cost the K = 1 kernel
+  // its third CTA per SM), 32 KB for FP32 engines evaluating 16 or more points
+  // (K = 64: 8.55 ms against 8.68 ms at 28 KB; beyond 32 KB the tiles' event
+  // and dial limits bind first), 40 KB for the 8-byte precisions (FP64
   // and double-float: fastest of 16-48 KB at K = 1 and K = 64; at 48 KB one
   // CTA per SM is left)
-  const int64_t tile_default = tsz == 4 ? 28672 : 40960;
+  const int64_t tile_default = tsz == 4 ? (e->cfg.k_max >= 16 ? 32768 : 28672) : 40960;
   int64_t cap_elems = (e->cfg.tile_bytes > 0 ? e->cfg.tile_bytes : tile_default) / (int64_t)tsz;
   cap_elems = std::min<int64_t>(cap_elems, kMaxPayloadElems);
   cap_elems = std::max<int64_t>(cap_elems, 64);

@@ -120,7 +120,8 @@ typedef struct gw_config {
   int32_t k_max;      /* largest number of parameter points per gw_eval (>= 1) */
   int32_t precision;  /* GW_FP64, GW_FP32 or GW_DF64 */
   int32_t device;     /* CUDA device ordinal */
-  int32_t tile_bytes; /* payload bytes per tile; 0 = default (28672 FP32, 40960 FP64 and double-float) */
+  int32_t tile_bytes; /* payload bytes per tile; 0 = default (FP32: 28672, 32768 with k_max >= 16;
+                         FP64 and double-float: 40960) */
   int32_t flags;      /* 0 or one GW_FLAG_SPLINE_* value */
 } gw_config;
 
