@@ -331,11 +331,38 @@ __global__ void __launch_bounds__(NEV + kWsRed, sizeof(T) == 4 ? 3 : 2) k_plain_
   } else {
     const int r = tid - kWsEval;
     const int rwarp = r >> 5, lane = r & 31;
+    // Reducer thread r handles events r, r + 64, ... of each tile.  The next
+    // tile's descriptor, its event words and this thread's base weights are
+    // loaded one tile ahead, so their latency overlaps the current tile's
+    // products and sums instead of opening each tile.
+    constexpr int kEvPer = kMaxTileEvents / kWsRed;
+    TileDesc tdn;
+    uint16_t pev[kEvPer];
+    T pw0[kEvPer];
+    auto prefetch = [&](int t) {
+      tdn = v.tiles[t];
+#pragma unroll
+      for (int j = 0; j < kEvPer; ++j) {
+        const int e = r + j * kWsRed;
+        if (e < (int)tdn.nevents) {
+          pev[j] = v.evinfo[tdn.event0 + e];
+          pw0[j] = ((const T*)v.w0)[tdn.event0 + e];
+        }
+      }
+    };
+    if (ntile > 0) prefetch(blockIdx.x);
     for (int it = 0; it < ntile; ++it) {
       const int tile = blockIdx.x + it * gridDim.x;
       const int b = it & 1;
-      const TileDesc td = v.tiles[tile];
-      for (int e = r; e < td.nevents; e += kWsRed) sev[e] = v.evinfo[td.event0 + e];
+      const TileDesc td = tdn;
+      T w0r[kEvPer];
+#pragma unroll
+      for (int j = 0; j < kEvPer; ++j) {
+        const int e = r + j * kWsRed;
+        if (e < (int)td.nevents) sev[e] = pev[j];
+        w0r[j] = pw0[j];
+      }
+      if (it + 1 < ntile) prefetch(tile + gridDim.x);
       if (r < kMaxLocalBins) {
         s_bstart[r] = 0;
         s_bend[r] = 0;
@@ -343,14 +370,17 @@ __global__ void __launch_bounds__(NEV + kWsRed, sizeof(T) == 4 ? 3 : 2) k_plain_
       named_sync(kBarRed, kWsRed);
       named_sync(kBarFull + b, NT);  // buffer b holds this tile's values
       const T* dv = dval + b * 1024;
-      for (int e = r; e < td.nevents; e += kWsRed) {
+#pragma unroll
+      for (int j = 0; j < kEvPer; ++j) {
+        const int e = r + j * kWsRed;
+        if (e >= (int)td.nevents) break;
         const uint16_t evi = sev[e];
         const int s0 = ev_slot(evi);
         const int s1 = (e + 1 < td.nevents) ? ev_slot(sev[e + 1]) : (int)td.ndials;
         T w = T(1);
         for (int q = s0; q < s1; ++q) w *= dv[q];
         if (v.has_cap && w > (T)v.cap) w = (T)v.cap;
-        w = ((const T*)v.w0)[td.event0 + e] * w;
+        w = w0r[j] * w;
         wsh[e] = (double)w;
         if (v.event_weights) v.event_weights[v.sorted_to_result[td.event0 + e]] = (double)w;
         const int lb = ev_lbin(evi);
