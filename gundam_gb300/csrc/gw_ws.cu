@@ -168,14 +168,37 @@ __global__ void __launch_bounds__(kSThreads, MB) k_ws(const DevView v, int K) {
     // ---------------- reducers ----------------
     const int r = tid - kSEval;
     const int rwarp = r >> 5, lane = r & 31;
+    // the next tile's descriptor, event words and base weights, loaded one
+    // tile ahead (reducer thread r stores events r, r + 64, ...)
+    constexpr int kEvPer = kMaxTileEvents / kSRed;
+    TileDesc tdn;
+    uint16_t pev[kEvPer];
+    T pw0[kEvPer];
+    auto prefetch = [&](int t) {
+      tdn = v.tiles[t];
+#pragma unroll
+      for (int j = 0; j < kEvPer; ++j) {
+        const int e = r + j * kSRed;
+        if (e < (int)tdn.nevents) {
+          pev[j] = v.evinfo[tdn.event0 + e];
+          pw0[j] = ((const T*)v.w0)[tdn.event0 + e];
+        }
+      }
+    };
+    if (ntile > 0) prefetch(blockIdx.x);
     for (int it = 0; it < ntile; ++it) {
       const int tile = blockIdx.x + it * gridDim.x;
-      const TileDesc td = v.tiles[tile];
+      const TileDesc td = tdn;
       const int ne = td.nevents;
-      for (int e = r; e < ne; e += kSRed) {
-        sev[e] = v.evinfo[td.event0 + e];
-        sw0[e] = ((const T*)v.w0)[td.event0 + e];
+#pragma unroll
+      for (int j = 0; j < kEvPer; ++j) {
+        const int e = r + j * kSRed;
+        if (e < ne) {
+          sev[e] = pev[j];
+          sw0[e] = pw0[j];
+        }
       }
+      if (it + 1 < ntile) prefetch(tile + gridDim.x);
       if (r == 0) sev[ne] = make_evinfo(td.ndials, 0);
       if (r < kMaxLocalBins) {
         s_bstart[r] = 0;
