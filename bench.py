@@ -496,11 +496,12 @@ def run_gw(args, world, rank, local, dist):
     plain_name = PLAIN_NAMES[eng.plain_kernel()]
     variants = {}
     if not args.no_variants:
-        # K = 1 (the plain kernel) on this engine, whose splines carry precomputed
-        # slopes for the batched kernel, and on a K = 1 engine (knot values)
+        # K = 1 (the plain kernel) on this engine, whose splines are stored in
+        # the batched kernel's form (the grid form at K >= 16), and on a K = 1
+        # engine (knot values)
         eng.autotune(1)
         ms1, kms1, _ = time_device(eng, torch, d, 1, args.steps, args.warmup, dist)
-        variants[f"{args.precision}_K1_slopes_layout"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
+        variants[f"{args.precision}_K1_batched_layout"] = {"kernel": PLAIN_NAMES[eng.plain_kernel()],
             "evals_per_s": 1e3 / ms1, "ms_per_eval": ms1, "kernel_ms": kms1,
             "kernel_gbs": algorithmic_bytes(wl, args.precision, 1) / (kms1 / 1e3) / 1e9,
             "payload_bytes": layout["payload_bytes"]}
@@ -539,11 +540,15 @@ def run_gw(args, world, rank, local, dist):
                 "payload_bytes": es.layout()["payload_bytes"]}
         es.close()
         if K > 16:
-            # C3 at the C2 size: K = 16 on this engine, K = 256 on one sized for it
-            eng.autotune(16)
-            ms16, kms16, _ = time_device(eng, torch, d, 16, args.steps, args.warmup, dist)
+            # C3 at the C2 size: K = 16 and K = 256 on engines sized for them
+            # (each with its default spline form)
+            e16 = Engine.from_workload(wl, precision=args.precision, k_max=16, llh_type=llh_type_for(args.config),
+                                       device=local)
+            e16.autotune(16)
+            ms16, kms16, _ = time_device(e16, torch, d, 16, args.steps, args.warmup, dist)
             variants[f"{args.precision}_K16"] = {"evals_per_s": 16e3 / ms16, "ms_per_step": ms16, "kernel_ms": kms16,
-                                                  "shape": list(eng.shape())}
+                                                  "shape": list(e16.shape())}
+            e16.close()
         if args.precision == "fp32":
             # the reference's precision (FP64) and the double-float mode (two
             # FP32 words per value on the FP32 pipe, sums and LLH in FP64, held

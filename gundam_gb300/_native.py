@@ -38,6 +38,7 @@ GW_DF64 = 2
 GW_FLAG_SPLINE_KNOTS = 1
 GW_FLAG_SPLINE_SLOPES = 2
 GW_FLAG_SPLINE_COEFS = 3
+GW_FLAG_SPLINE_GRID = 4
 
 GW_LLH_NONE = 0
 GW_LLH_POISSON = 1

@@ -109,6 +109,24 @@ __device__ __forceinline__ void issue_tile_hdr(const DevView& v, int tile, unsig
   if (hbytes > 0) bulk_load(hbuf, v.hdr + td.dial0, hbytes, bar);
 }
 
+// DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18): a
+// response below lo becomes lo, above hi becomes hi, anything else (NaN
+// included) passes.  In FP32 that is the NaN-propagating max then min, two
+// instructions instead of two compare-and-select pairs (with lo <= hi, which
+// the builder checks).
+template <typename T>
+__device__ __forceinline__ T clamp_response(T r, T lo, T hi) {
+  if (r < lo) r = lo;
+  else if (r > hi) r = hi;
+  return r;
+}
+__device__ __forceinline__ float clamp_response(float r, float lo, float hi) {
+  float t;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(t) : "f"(r), "f"(lo));
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(t) : "f"(t), "f"(hi));
+  return t;
+}
+
 // ---------------------------------------------------------------------------
 // One dial at KR parameter points (k0, k0 + kstep, ...): the header is
 // decoded, the type dispatched and the response clamp loaded once; the KR
@@ -143,11 +161,15 @@ __device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, 
 }
 
 // The KR values of one parameter at points k0, k0 + kstep, ...  With VX the
-// points are contiguous (kstep == 1) and k0 * sizeof(T) is a multiple of 16,
-// so whole 16-byte vectors are loaded.
+// points are contiguous (kstep == 1) and k0 * sizeof(T) is a multiple of
+// KR * sizeof(T) (at most 16), so whole 8- or 16-byte vectors are loaded.
 template <typename T, int KR, bool VX>
 __device__ __forceinline__ void load_points(const T* __restrict__ p, int kstep, T (&x)[KR]) {
-  if constexpr (VX && (KR * sizeof(T)) % 16 == 0) {
+  if constexpr (VX && KR == 2 && sizeof(T) == 4) {
+    const float2 f = *reinterpret_cast<const float2*>(p);  // k0 even: 8-byte aligned
+    x[0] = f.x;
+    x[1] = f.y;
+  } else if constexpr (VX && (KR * sizeof(T)) % 16 == 0) {
     if constexpr (kIsDf<T>) {
       const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
@@ -189,6 +211,29 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
   const T* d = pl + hdr_off(h);
   const int p0 = hdr_p0(h);
   T lo, hi;
+  if (type == kGrid) {
+    // the grid form: interval and fraction per point from k_params, the
+    // response clamp per grid (already within [-1e20, 1e20])
+    const GridPoint<T>* gp = (const GridPoint<T>*)v.grid_pts + (size_t)p0 * v.kpad + k0;
+    const typename Vec2<T>::type c = ((const typename Vec2<T>::type*)v.grid_clamp)[p0];
+    if constexpr (VX && sizeof(GridPoint<T>) == 8 && KR % 2 == 0) {
+      // contiguous points, k0 even: two 8-byte entries per 16-byte load
+      const float4* q = reinterpret_cast<const float4*>(gp);
+#pragma unroll
+      for (int j = 0; j < KR; j += 2) {
+        const float4 f = q[j / 2];
+        val[j] = clamp_response(coef_cubic(d + __float_as_int(f.y), (T)f.x), c.x, c.y);
+        val[j + 1] = clamp_response(coef_cubic(d + __float_as_int(f.w), (T)f.z), c.x, c.y);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < KR; ++j) {
+        const GridPoint<T> g = gp[j * kstep];
+        val[j] = clamp_response(coef_cubic(d + g.jb, g.u), c.x, c.y);
+      }
+    }
+    return;
+  }
   if (type >= kTabulated) {
     // Tabulated.h:27-28 and Kriged.cpp:14-21; clamp of the table's dials.
     const TableDesc td = v.tables[p0];
@@ -225,8 +270,13 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       // Spline, graph and surface responses: Calculate*.h clamps to
       // [-1e20, 1e20] before the response clamp; with lower <= upper the two
       // clamps are one clamp to the intersection.
-      if (lo < T(-1e20)) lo = T(-1e20);
-      if (hi > T(1e20)) hi = T(1e20);
+      if constexpr (sizeof(T) == 4) {  // lo, hi are never NaN
+        lo = fmaxf(lo, -1e20f);
+        hi = fminf(hi, 1e20f);
+      } else {
+        if (lo < T(-1e20)) lo = T(-1e20);
+        if (hi > T(1e20)) hi = T(1e20);
+      }
       // the stored spline form is checked inside each spline type's branch,
       // so the other types pay nothing for it
       if (type == kMonotonic) {
@@ -275,12 +325,8 @@ __device__ __forceinline__ void dial_values(const DevView& v, uint64_t h, const 
       }
     }
   }
-  // DialResponseSupervisor::process (DialResponseSupervisor.cpp:10-18)
 #pragma unroll
-  for (int j = 0; j < KR; ++j) {
-    if (val[j] < lo) val[j] = lo;
-    else if (val[j] > hi) val[j] = hi;
-  }
+  for (int j = 0; j < KR; ++j) val[j] = clamp_response(val[j], lo, hi);
 }
 
 // Per-bin likelihoods.

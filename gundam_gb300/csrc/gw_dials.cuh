@@ -287,9 +287,11 @@ __device__ __forceinline__ void eval_prepared2(const float* __restrict__ d, int 
 // the last knot, re-expanded about their own origin), so no end rule is
 // applied here.  With truncation xx is first clamped to [0, n - 1] (the end
 // knots' values).  The coefficient blocks are 16-byte aligned.
+// The interval of xx = (x - low) / step in the coefficient form: with
+// truncation xx is first clamped to [0, n - 1]; j = clamp(floor(xx), -1,
+// n - 1) and u = xx - j.  Returns j + 1, the index of the coefficient block.
 template <typename T>
-__device__ __forceinline__ T eval_coef(const T* __restrict__ d, int n, T x, bool trunc) {
-  T xx = x * d[1] + d[0];
+__device__ __forceinline__ int coef_interval(T& xx, int n, bool trunc, T& u) {
   if (trunc) xx = (xx < T(0)) ? T(0) : ((xx > T(n - 1)) ? T(n - 1) : xx);
   int j;
   T fj;
@@ -305,9 +307,34 @@ __device__ __forceinline__ T eval_coef(const T* __restrict__ d, int n, T x, bool
     fj = T(i);
     j = i + 1;
   }
-  const T u = xx - fj;
-  const T* c = d + 4 + 4 * j;
+  u = xx - fj;
+  return j;
+}
+
+// The cubic of one coefficient block at u.
+template <typename T>
+__device__ __forceinline__ T coef_cubic(const T* __restrict__ c, T u) {
   return c[0] + u * (c[1] + u * (c[2] + u * c[3]));
+}
+__device__ __forceinline__ float coef_cubic(const float* __restrict__ c, float u) {
+  const float4 q = *(const float4*)c;  // blocks are 16-byte aligned
+  return q.x + u * (q.y + u * (q.z + u * q.w));
+}
+
+// Uniform-knot splines in the coefficient form (GW_FLAG_SPLINE_COEFS):
+// d = [-low/step, 1/step, 0, 0, (c0, c1, c2, c3) x (n + 1)].  xx = (x - low)
+// / step as one multiply-add, j = clamp(floor(xx), -1, n - 1), u = xx - j,
+// and the block j + 1 holds the cubic of u on that interval (the blocks of
+// j = -1 and j = n - 1 hold the reference's extrapolation beyond the first and
+// the last knot, re-expanded about their own origin), so no end rule is
+// applied here.  With truncation xx is first clamped to [0, n - 1] (the end
+// knots' values).  The coefficient blocks are 16-byte aligned.
+template <typename T>
+__device__ __forceinline__ T eval_coef(const T* __restrict__ d, int n, T x, bool trunc) {
+  T xx = x * d[1] + d[0];
+  T u;
+  const int j = coef_interval(xx, n, trunc, u);
+  return coef_cubic(d + 4 + 4 * j, u);
 }
 
 // The same at two points (FP32): one 16-byte load per point, the index and

@@ -225,7 +225,7 @@ extern "C" int gw_create(const gw_config* c, gw_engine** out) {
   if (c->n_results < 0 || c->n_params < 1 || c->n_params > 8192 || c->n_bins < 1 || c->k_max < 1 ||
       c->k_max > 4096 || (c->precision != GW_FP64 && c->precision != GW_FP32 && c->precision != GW_DF64) ||
       (c->flags != 0 && c->flags != GW_FLAG_SPLINE_KNOTS && c->flags != GW_FLAG_SPLINE_SLOPES &&
-       c->flags != GW_FLAG_SPLINE_COEFS))
+       c->flags != GW_FLAG_SPLINE_COEFS && c->flags != GW_FLAG_SPLINE_GRID))
     return fail(nullptr, GW_ERR_ARG,
                 "bad gw_config (n_results=%d n_params=%d n_bins=%d k_max=%d precision=%d flags=%d)",
                 c->n_results, c->n_params, c->n_bins, c->k_max, c->precision, c->flags);
@@ -696,7 +696,7 @@ static void knot_slopes(const DialRec& r, const double* d, int n, double* y, dou
 }
 
 // Stored form of a spline's Catmull-Rom or Hermite data (SplineForm).
-enum SplineForm { kFormSlopes = 0, kFormKnots = 1, kFormCoefs = 2 };
+enum SplineForm { kFormSlopes = 0, kFormKnots = 1, kFormCoefs = 2, kFormGrid = 3 };
 
 // Engine layout of Catmull-Rom (monotonic, compact) and uniform splines.
 // Slopes form: [low, 1/step, (y, s) x n], s the knot slope in index units
@@ -705,7 +705,9 @@ enum SplineForm { kFormSlopes = 0, kFormKnots = 1, kFormCoefs = 2 };
 template <typename T>
 void write_prepared(const DialRec& r, const double* d, int n, T* out, int form) {
   const double low = d[0], step = d[1];
-  if (form == kFormCoefs) {
+  if (form == kFormCoefs || form == kFormGrid) {
+    // the grid form keeps the blocks alone: [(c0, c1, c2, c3) x (n + 1)]
+    const int b0 = form == kFormGrid ? 0 : 4;
     // [-low/step, 1/step, 0, 0, (c0, c1, c2, c3) x (n + 1)]: interval j + 1
     // holds the cubic v(u) = c0 + u (c1 + u (c2 + u c3)) of u = xx - j, xx =
     // (x - low) / step, for j = -1 .. n - 1.  j = 0 .. n - 2 are the Hermite
@@ -724,14 +726,16 @@ void write_prepared(const DialRec& r, const double* d, int n, T* out, int form) 
       c[2] = 3.0 * dc - 2.0 * m1 - m2;
       c[3] = m1 + m2 - 2.0 * dc;
     };
-    out[0] = (T)(-low / step);
-    out[1] = (T)(1.0 / step);
-    out[2] = (T)0.0;
-    out[3] = (T)0.0;
+    if (form == kFormCoefs) {
+      out[0] = (T)(-low / step);
+      out[1] = (T)(1.0 / step);
+      out[2] = (T)0.0;
+      out[3] = (T)0.0;
+    }
     double c[4];
     for (int j = 0; j + 1 < n; ++j) {
       cubic(j, sl[(size_t)j], sl[(size_t)j + 1], c);
-      for (int q = 0; q < 4; ++q) out[4 + 4 * (j + 1) + q] = (T)c[q];
+      for (int q = 0; q < 4; ++q) out[b0 + 4 * (j + 1) + q] = (T)c[q];
     }
     // before the first knot: P(t), t = xx, as P(u - 1)
     cubic(0, sl[0], catmull ? y[1] - y[0] : sl[1], c);
@@ -740,8 +744,8 @@ void write_prepared(const DialRec& r, const double* d, int n, T* out, int form) 
     cubic(n - 2, catmull ? y[(size_t)n - 1] - y[(size_t)n - 2] : sl[(size_t)n - 2], sl[(size_t)n - 1], c);
     const double right[4] = {c[0] + c[1] + c[2] + c[3], c[1] + 2.0 * c[2] + 3.0 * c[3], c[2] + 3.0 * c[3], c[3]};
     for (int q = 0; q < 4; ++q) {
-      out[4 + q] = (T)left[q];
-      out[4 + 4 * n + q] = (T)right[q];
+      out[b0 + q] = (T)left[q];
+      out[b0 + 4 * n + q] = (T)right[q];
     }
     return;
   }
@@ -765,6 +769,7 @@ void write_prepared(const DialRec& r, const double* d, int n, T* out, int form) 
 int32_t stored_elems(const DialRec& r, int n, int32_t raw, int form) {
   const bool uniform_knots = r.type == kMonotonic || r.type == kCompact || r.type == kUniform;
   if (form == kFormCoefs && uniform_knots) return 4 + 4 * (n + 1);  // 16-byte multiple, packed first
+  if (form == kFormGrid && uniform_knots) return 4 * (n + 1);
   int32_t el = (r.type == kMonotonic || r.type == kCompact) ? (form == kFormKnots ? 2 + n : 2 + 2 * n) : raw;
   if (el > 0 && (el & 1) == 0) ++el;
   return el;
@@ -786,18 +791,28 @@ int build_and_upload(gw_engine* e) {
   const int B = e->cfg.n_bins;
   const int64_t D = (int64_t)e->dials.size();
   const size_t tsz = sizeof(T);
-  // stored form of Catmull-Rom splines (gw_config.flags; by default knot
-  // values for FP32 K = 1 engines, precomputed slopes otherwise)
-  // default: knot values for FP32 K = 1 engines (bandwidth-bound), the
-  // coefficient form for FP64 engines evaluating 16 or more points (their
-  // batched kernel is bound by the FP64 pipe: 92 ms against 124 ms for 64
-  // points of the 5M-event mixed workload), precomputed slopes otherwise
-  const int form = e->cfg.flags == GW_FLAG_SPLINE_KNOTS    ? kFormKnots
-                   : e->cfg.flags == GW_FLAG_SPLINE_COEFS   ? kFormCoefs
-                   : e->cfg.flags == GW_FLAG_SPLINE_SLOPES  ? kFormSlopes
-                   : (e->cfg.k_max == 1 && tsz == 4)        ? kFormKnots
-                   : (e->cfg.precision == GW_FP64 && e->cfg.k_max >= 16) ? kFormCoefs
-                                                                          : kFormSlopes;
+  // stored form of the uniform-knot splines (gw_config.flags).  Default:
+  // knot values for FP32 K = 1 engines (bandwidth-bound); the grid form for
+  // engines evaluating 32 or more points, where the lanes-over-points kernel
+  // runs (64 points of a 2M-event mixed workload: FP32 2.74 ms against
+  // 3.27 ms with stored slopes, FP64 12.3 ms against 18.8 ms with the
+  // coefficient form).  At 16-31 points the threads-over-dials kernels win,
+  // and their scattered per-dial reads of the grid table pay only while the
+  // table stays in L1 (FP32, 16 points: a 100k-event workload with 20 grids
+  // 0.054 ms against 0.072 ms with stored slopes; the 2M-event workload with
+  // 400 grids 2.48 ms against 1.84 ms), so there the grid form is kept when
+  // the table holds at most 32 KB, else FP64 engines take the coefficient
+  // form (their evaluation is bound by the FP64 pipe) and the others stored
+  // slopes; precomputed slopes otherwise
+  const int form_small = (e->cfg.precision == GW_FP64) ? kFormCoefs : kFormSlopes;
+  const bool grid_if_small = e->cfg.flags == 0 && e->cfg.k_max >= 16 && e->cfg.k_max < 32;
+  int form = e->cfg.flags == GW_FLAG_SPLINE_KNOTS           ? kFormKnots
+             : e->cfg.flags == GW_FLAG_SPLINE_COEFS         ? kFormCoefs
+             : e->cfg.flags == GW_FLAG_SPLINE_GRID          ? kFormGrid
+             : e->cfg.flags == GW_FLAG_SPLINE_SLOPES        ? kFormSlopes
+             : (e->cfg.k_max == 1 && tsz == 4)              ? kFormKnots
+             : (e->cfg.k_max >= 32 || grid_if_small)        ? kFormGrid
+                                                            : kFormSlopes;
 
   // 1. every result needs a bin (CacheManager.cpp:727-729 "Histogram cells are missing")
   for (int r = 0; r < N; ++r)
@@ -820,6 +835,94 @@ int build_and_upload(gw_engine* e) {
     std::vector<int64_t> fillp(rstart.begin(), rstart.end() - 1);
     for (int64_t i = 0; i < D; ++i) byres[(size_t)fillp[e->dials[(size_t)i].result]++] = i;
   }
+  // the grid form: uniform-knot splines that share (parameter, first knot,
+  // step, knot count) share one knot grid, whose interval and fraction
+  // k_params forms once per point; up to kMaxGrids grids in first-seen
+  // order, the splines of any further grid keep the coefficient form
+  std::vector<int32_t> grid_of;
+  std::vector<GridDesc> grids;
+  if (form == kFormGrid) {
+    grid_of.assign((size_t)D, -1);
+    struct Key {
+      int32_t p0, n;
+      double low, step;
+      bool operator<(const Key& o) const {
+        if (p0 != o.p0) return p0 < o.p0;
+        if (n != o.n) return n < o.n;
+        if (low != o.low) return low < o.low;
+        return step < o.step;
+      }
+    };
+    auto key_of = [&](const DialRec& r, Key* k) {
+      if (r.type != kMonotonic && r.type != kCompact && r.type != kUniform) return false;
+      const double* d = e->dial_data.data() + r.data_off;
+      const int n = r.type == kUniform ? (r.n_data - 2) / 2 : r.n_data - 2;
+      if (n < 2 || n > kMaxKnots || !(d[1] > 0.0) || !std::isfinite(d[0]) || !std::isfinite(d[1])) return false;
+      *k = Key{r.p0, n, d[0], d[1]};
+      return true;
+    };
+    // each thread names the grids of its dials locally; the local names are
+    // then merged in first-seen order of the dials
+    const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    const int64_t chunk = (D + nth - 1) / std::max(nth, 1);
+    std::vector<std::map<Key, int32_t>> local((size_t)nth);
+    std::vector<std::vector<std::pair<int64_t, Key>>> first((size_t)nth);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) {
+      th.emplace_back([&, t]() {
+        for (int64_t i = t * chunk; i < std::min<int64_t>(D, (t + 1) * chunk); ++i) {
+          Key k;
+          if (!key_of(e->dials[(size_t)i], &k)) continue;
+          auto it = local[(size_t)t].find(k);
+          if (it == local[(size_t)t].end()) {
+            it = local[(size_t)t].emplace(k, (int32_t)first[(size_t)t].size()).first;
+            first[(size_t)t].emplace_back(i, k);
+          }
+          grid_of[(size_t)i] = it->second;
+        }
+      });
+    }
+    for (auto& x : th) x.join();
+    th.clear();
+    std::map<Key, int32_t> global;
+    std::vector<std::vector<int32_t>> to_global((size_t)nth);
+    for (int t = 0; t < nth; ++t) {
+      for (const auto& f : first[(size_t)t]) {
+        auto it = global.find(f.second);
+        int32_t g = -1;
+        if (it != global.end()) {
+          g = it->second;
+        } else if ((int)grids.size() < kMaxGrids) {
+          g = (int32_t)grids.size();
+          global.emplace(f.second, g);
+          GridDesc gd{};
+          gd.a = -f.second.low / f.second.step;
+          gd.b = 1.0 / f.second.step;
+          gd.p0 = f.second.p0;
+          gd.n = f.second.n;
+          gd.trunc = (e->pflags[(size_t)f.second.p0] & 1) ? 1 : 0;
+          grids.push_back(gd);
+        }
+        to_global[(size_t)t].push_back(g);
+      }
+    }
+    for (int t = 0; t < nth; ++t) {
+      th.emplace_back([&, t]() {
+        for (int64_t i = t * chunk; i < std::min<int64_t>(D, (t + 1) * chunk); ++i)
+          if (grid_of[(size_t)i] >= 0) grid_of[(size_t)i] = to_global[(size_t)t][(size_t)grid_of[(size_t)i]];
+      });
+    }
+    for (auto& x : th) x.join();
+    const int64_t kpad_of = ((e->cfg.k_max + 63) / 64) * 64;
+    if (grid_if_small && (int64_t)grids.size() * kpad_of * (int64_t)sizeof(GridPoint<T>) > 32768) {
+      form = form_small;
+      grids.clear();
+      grid_of.clear();
+    }
+  }
+  // the stored form of the uniform-knot splines outside the grids
+  const int dial_form = form == kFormGrid ? kFormCoefs : form;
+
   // per-dial payload sizes and knot counts
   std::vector<int32_t> pel((size_t)D), pn((size_t)D);
   {
@@ -836,7 +939,8 @@ int build_and_upload(gw_engine* e) {
             int64_t exp = -1;
             bad.compare_exchange_strong(exp, i);
           }
-          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, form);
+          const int f = (!grid_of.empty() && grid_of[(size_t)i] >= 0) ? kFormGrid : dial_form;
+          pel[(size_t)i] = el < 0 ? -1 : stored_elems(r, n, (int32_t)el, f);
           pn[(size_t)i] = n;
         }
       });
@@ -954,6 +1058,7 @@ int build_and_upload(gw_engine* e) {
   std::vector<uint64_t> hdr((size_t)hdr_total, 0);
   std::vector<unsigned char> payload((size_t)payload_total, 0);
   std::vector<uint16_t> evinfo((size_t)N);
+  std::vector<uint16_t> evcost((size_t)N);
   std::vector<T> w0((size_t)N);
   {
     const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
@@ -964,12 +1069,22 @@ int build_and_upload(gw_engine* e) {
         std::vector<int32_t> order;
         for (int64_t ti = t; ti < T_; ti += nth) {
           const TilePlan& tp = tiles[(size_t)ti];
+          auto htype = [&](int64_t di) {
+            return (!grid_of.empty() && grid_of[(size_t)di] >= 0) ? (int)kGrid : (int)e->dials[(size_t)di].type;
+          };
           ev_major.clear();
+          int cost = 0;
           for (int64_t i = tp.ev_begin; i < tp.ev_end; ++i) {
             const int r = sorted[(size_t)i];
             evinfo[(size_t)i] = make_evinfo((int)ev_major.size(), e->bin[r] - tp.bin0);
             w0[(size_t)i] = (T)e->initial[r];
-            for (int64_t j = rstart[r]; j < rstart[r + 1]; ++j) ev_major.push_back(byres[(size_t)j]);
+            cost += kEventCost;
+            for (int64_t j = rstart[r]; j < rstart[r + 1]; ++j) {
+              const int64_t di = byres[(size_t)j];
+              ev_major.push_back(di);
+              cost += dial_cost(htype(di), pn[(size_t)di]);
+            }
+            evcost[(size_t)i] = (uint16_t)cost;
           }
           const int nd = (int)ev_major.size();
           order.resize(nd);
@@ -977,8 +1092,9 @@ int build_and_upload(gw_engine* e) {
           // type order; in the coefficient form the three uniform-knot spline
           // types first, so their 16-byte-multiple payloads start 16-byte aligned
           auto key = [&](int a) {
-            const int ty = e->dials[(size_t)ev_major[a]].type;
-            const bool first = form == kFormCoefs && (ty == kMonotonic || ty == kCompact || ty == kUniform);
+            const int ty = htype(ev_major[a]);
+            const bool first = dial_form == kFormCoefs &&
+                               (ty == kMonotonic || ty == kCompact || ty == kUniform || ty == kGrid);
             return (first ? 0 : 16) + ty;
           };
           std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
@@ -988,11 +1104,14 @@ int build_and_upload(gw_engine* e) {
             const int slot = order[j];
             const int64_t di = ev_major[slot];
             const DialRec& r = e->dials[(size_t)di];
-            const int p0 = r.type >= kTabulated ? (int)e->dial_data[(size_t)r.data_off] : r.p0;
+            const int g = grid_of.empty() ? -1 : grid_of[(size_t)di];
+            const int p0 = g >= 0 ? g : r.type >= kTabulated ? (int)e->dial_data[(size_t)r.data_off] : r.p0;
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
-            hdr[(size_t)(tp.dial0 + j)] = make_header(r.type, pn[(size_t)di], slot, off, p0, p1);
+            hdr[(size_t)(tp.dial0 + j)] = make_header(g >= 0 ? (int)kGrid : (int)r.type, pn[(size_t)di], slot, off,
+                                                      p0, p1);
             if (r.type == kMonotonic || r.type == kCompact || r.type == kUniform)
-              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off, form);
+              write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off,
+                                g >= 0 ? kFormGrid : dial_form);
             else
               write_payload<T>(r, e->dial_data.data() + r.data_off, pl + off);
             off += pel[(size_t)di];
@@ -1064,8 +1183,8 @@ int build_and_upload(gw_engine* e) {
   v.cap = e->cap;
   v.tile_payload_bytes = (int)(((cap_elems * tsz) + 127) & ~(int64_t)127);
   v.tile_hdr_bytes = std::max(16, ((max_tile_dials + 1) / 2) * 16);
-  v.spline_knots = form == kFormKnots ? 1 : 0;
-  v.spline_coefs = form == kFormCoefs ? 1 : 0;
+  v.spline_knots = dial_form == kFormKnots ? 1 : 0;
+  v.spline_coefs = dial_form == kFormCoefs ? 1 : 0;
 
   // slack after the per-dial and per-event arrays (reads rounded out to
   // 16-byte boundaries stay inside the allocation)
@@ -1080,6 +1199,9 @@ int build_and_upload(gw_engine* e) {
   v.payload = (const unsigned char*)p;
   if ((rc = upload(evinfo.data(), evinfo.size() * sizeof(uint16_t), &p))) return rc;
   v.evinfo = (const uint16_t*)p;
+  evcost.resize(evcost.size() + 8, 0);
+  if ((rc = upload(evcost.data(), evcost.size() * sizeof(uint16_t), &p))) return rc;
+  v.evcost = (const uint16_t*)p;
   if ((rc = upload(w0.data(), w0.size() * sizeof(T), &p))) return rc;
   v.w0 = p;
   if ((rc = upload(bin_slot.data(), bin_slot.size() * sizeof(int32_t), &p))) return rc;
@@ -1173,6 +1295,32 @@ int build_and_upload(gw_engine* e) {
     v.n_tables = (int)td.size();
     v.n_table_fns = (int)fns.size();
     for (HostTable& h : e->tables) h.dirty = !h.has_fn;
+  }
+  // knot grids of the grid form, their response clamps (the parameter's,
+  // intersected with [-1e20, 1e20] in the engine precision, as the kernels do
+  // for the other dials) and the per-point intervals k_params forms
+  v.n_grids = (int)grids.size();
+  if (!grids.empty()) {
+    if ((rc = upload(grids.data(), grids.size() * sizeof(GridDesc), &p))) return rc;
+    v.grids = (const GridDesc*)p;
+    std::vector<T> gc(2 * grids.size());
+    for (size_t g = 0; g < grids.size(); ++g) {
+      const int q = grids[g].p0;
+      double lo = e->clamp_lo[(size_t)q], hi = e->clamp_hi[(size_t)q];
+      if (tsz == 4) {
+        lo = std::max(lo, -(double)FLT_MAX);
+        hi = std::min(hi, (double)FLT_MAX);
+      }
+      // the conversion to T is monotone, so clamping before it equals
+      // clamping after it
+      gc[2 * g] = (T)std::max(lo, -1e20);
+      gc[2 * g + 1] = (T)std::min(hi, 1e20);
+    }
+    if ((rc = upload(gc.data(), gc.size() * sizeof(T), &p))) return rc;
+    v.grid_clamp = p;
+    if ((rc = alloc(grids.size() * (size_t)kpad * sizeof(GridPoint<T>), &p))) return rc;
+    GW_CUDA(e, cudaMemset(p, 0, grids.size() * (size_t)kpad * sizeof(GridPoint<T>)));
+    v.grid_pts = p;
   }
   e->sorted_to_result = sorted;
   if ((rc = upload(sorted.data(), sorted.size() * sizeof(int32_t), &p))) return rc;

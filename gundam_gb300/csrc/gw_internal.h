@@ -31,12 +31,14 @@ struct DevView {
   int tile_hdr_bytes;      // shared-memory bytes for one tile's headers (16-byte multiple)
   int spline_knots;        // 1: Catmull-Rom payloads hold knot values only (slopes formed on the device)
   int spline_coefs;        // 1: monotonic, compact and uniform splines hold per-interval cubic coefficients
+  int n_grids;             // knot grids of the grid form (0: none)
   double cap;
 
   const TileDesc* tiles;
   const uint64_t* hdr;
   const unsigned char* payload;
   const uint16_t* evinfo;
+  const uint16_t* evcost;     // [n_events] summed dial_cost + kEventCost through the event, from its tile's first
   const void* w0;             // T[n_events], bin-sorted
   const int32_t* bin_slot;    // [n_bins + 1]
   const void* pclamp;         // T2[n_params] = (lower, upper)
@@ -58,6 +60,9 @@ struct DevView {
   const double* table_nodes;
   void* table_arena;          // T
   const int32_t* sorted_to_result;  // [n_events]
+  const GridDesc* grids;      // [n_grids]
+  const void* grid_clamp;     // T2[n_grids]: response clamp of the grid's dials, within [-1e20, 1e20]
+  void* grid_pts;             // GridPoint<T>[n_grids * kpad], formed by k_params
 
   void* x;                    // T[n_params * kpad], mirrored parameter values
   double* penalty;            // [kpad]

@@ -68,6 +68,19 @@ __global__ void __launch_bounds__(256) k_params(const DevView v, const double* _
     }
     xs[(size_t)p * v.kpad + k] = (T)x;
   }
+  if (v.n_grids > 0) {
+    // the grid form: interval and fraction of every knot grid at this point,
+    // the operations eval_coef applies per dial
+    __syncthreads();
+    GridPoint<T>* gp = (GridPoint<T>*)v.grid_pts;
+    for (int g = threadIdx.x; g < v.n_grids; g += blockDim.x) {
+      const GridDesc gd = v.grids[g];
+      T xx = xs[(size_t)gd.p0 * v.kpad + k] * (T)gd.b + (T)gd.a;
+      GridPoint<T> r;
+      r.jb = 4 * coef_interval(xx, gd.n, gd.trunc != 0, r.u);
+      gp[(size_t)g * v.kpad + k] = r;
+    }
+  }
   if (!v.has_prior) return;
   // delta^T C^-1 delta on the parameters as given (the eigen parameters of
   // decomposed blocks, as the reference's penalty in eigen mode), u = C^-1
@@ -498,7 +511,7 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
   const int nw = b.threads / 32;
   return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
          (size_t)(nw + kMaxLocalBins - 1) * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
-         (kMaxTileEvents + 1) * sizeof(uint16_t);
+         2 * (kMaxTileEvents + 1) * sizeof(uint16_t);
 }
 
 template <typename T>

@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
   double2* wpart = (double2*)(shdr + 1024);                   // [NE][KR][32]
   T* sw0 = (T*)(wpart + NE * KR * 32);                        // [256]
   uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
+  uint16_t* sec = sev + (kMaxTileEvents + 1);                 // [257]: work before each event, total last
   __shared__ uint64_t bar[2];
   __shared__ int s_present[kMaxLocalBins];
   __shared__ int s_run[NW][2];  // first, last local bin of each warp's run (first > last: none)
@@ -61,36 +62,45 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
     }
     for (int e = tid; e < ne; e += NT) {
       sev[e] = v.evinfo[td.event0 + e];
+      sec[e + 1] = v.evcost[td.event0 + e];
       sw0[e] = ((const T*)v.w0)[td.event0 + e];
     }
-    if (tid == 0) sev[ne] = make_evinfo(nd, 0);
+    if (tid == 0) {
+      sev[ne] = make_evinfo(nd, 0);
+      sec[0] = 0;
+    }
     if (tid < kMaxLocalBins) s_present[tid] = 0;
     const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicOr(v.status, kStatusCopyTimeout);
+        // the copies still pending: the next stage's, or with one stage the
+        // one that timed out; one more bounded wait each before exiting
         if (ST == 2 && next < v.n_tiles)
           mbar_wait_bounded(&bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimitNs);
+        if (ST == 1) mbar_wait_bounded(&bar[0], parity, kWaitLimitNs);
       }
       return;
     }
     for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
     const T* pl = (const T*)(st ? stage1 : stage0);
 
-    // Each warp takes a contiguous run of events holding ~nd/NW dials: the
-    // first event whose first slot reaches warp*nd/NW (a fixed, deterministic
-    // split, so the FP64 summation order does not depend on scheduling).
+    // Each warp takes a contiguous run of events holding ~1/NW of the tile's
+    // estimated work (dial_cost): the first event whose preceding work
+    // reaches warp*total/NW (a fixed, deterministic split, so the FP64
+    // summation order does not depend on scheduling).
     auto first_event_at = [&](int target) {
-      int lo = 0, hi = ne;  // sev[ne] holds nd
+      int lo = 0, hi = ne;  // sec[ne] holds the total
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (ev_slot(sev[mid]) < target) lo = mid + 1;
+        if ((int)sec[mid] < target) lo = mid + 1;
         else hi = mid;
       }
       return lo;
     };
-    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * nd) / NW);
-    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * nd) / NW);
+    const int total = sec[ne];
+    const int e_lo = (warp == 0) ? 0 : first_event_at((warp * total) / NW);
+    const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * total) / NW);
     const int b_first = (e_lo < e_hi) ? ev_lbin(sev[e_lo]) : 1;
     const int b_last = (e_lo < e_hi) ? ev_lbin(sev[e_hi - 1]) : 0;
     if (lane == 0) {
@@ -149,6 +159,9 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
         for (int j = 0; j < KR; ++j) wpart[((warp + cur) * KR + j) * 32 + lane] = make_double2(s[j], s2[j]);
       }
       __syncthreads();
+      // one stage: after the last pass nothing reads the payload any more, so
+      // the next tile's copy overlaps this tile's reduction
+      if (ST == 1 && kb + KP >= K && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
       for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
         const int lb = t / KP, r = t % KP;
         const int j = r / KC, kk = r % KC;
@@ -170,7 +183,6 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
       }
       __syncthreads();
     }
-    if (ST == 1 && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
   }
 }
 

@@ -27,6 +27,7 @@ constexpr int kMaxLocalBins = 4;      // bins spanned by one tile (bin - bin0 < 
 constexpr int kMaxPayloadElems = 8191; // 13-bit element offset
 constexpr int kMaxKnots = 31;         // 5-bit count field
 constexpr int kTypeCount = 11;
+constexpr int kMaxGrids = 16384;      // knot grids of the grid form (p0 field of the header)
 
 // Dial type codes (same numbering as the public GW_DIAL_* enum).
 enum : int {
@@ -40,7 +41,12 @@ enum : int {
   kBilinear = 7,
   kBicubic = 8,
   kTabulated = 9,
-  kKriged = 10
+  kKriged = 10,
+  // Header-only code (never a public dial type): a monotonic, compact or
+  // uniform spline of the grid form, whose knot grid (parameter, first knot,
+  // step, knot count) it shares with other dials.  Its header's p0 field holds
+  // the grid's index, its payload the per-interval cubic coefficients alone.
+  kGrid = 11
 };
 
 // 64-bit dial header:
@@ -62,6 +68,31 @@ GW_HD int hdr_off(uint64_t h) { return (int)((h >> 19) & 0x1FFF); }
 GW_HD int hdr_p0(uint64_t h) { return (int)((h >> 32) & 0xFFFF); }
 GW_HD int hdr_p1(uint64_t h) { return (int)((h >> 48) & 0xFFFF); }
 
+// Relative work of one dial in the lanes-over-points kernel (about ten warp
+// instructions per unit at 64 points, from instruction counts of one-type
+// workloads), and of one event's product and sums.  A tile's warps take runs
+// of events of equal summed work, not of equal dial count: the dial types
+// differ in cost by up to ten times, and the warps of a tile wait for the
+// slowest at the tile's barrier.  A tile's total stays below 2^16
+// (kMaxTileDials * 40 + kMaxTileEvents * kEventCost).
+GW_HD int dial_cost(int type, int n) {
+  switch (type) {
+    case kNorm: return 3;
+    case kGrid: return 7;
+    case kMonotonic:
+    case kCompact:
+    case kUniform: return 14;
+    case kGeneral: return 19;
+    case kGraph: return 15;
+    case kBilinear: return 30;
+    case kBicubic: return 40;
+    case kTabulated: return 6;
+    case kKriged: return 4 + (n < 31 ? n : 31);
+    default: return 3;
+  }
+}
+constexpr int kEventCost = 10;
+
 // 16-bit per-event word: [0,10) first slot of the event, [10,13) local bin.
 GW_HD uint16_t make_evinfo(int slot0, int lbin) {
   return (uint16_t)((slot0 & 0x3FF) | ((lbin & 0x7) << 10));
@@ -81,6 +112,29 @@ struct TileDesc {
   uint16_t nbins;         // bin span: 1 + (last bin - bin0)
 };
 static_assert(sizeof(TileDesc) == 32, "TileDesc must stay 32 bytes");
+
+// A knot grid shared by uniform-knot splines (the grid form): for every
+// evaluated point k, the kernel that mirrors the parameters also forms
+// xx = x[p0][k] * b + a (a = -low/step, b = 1/step in the engine precision),
+// clamps it to [0, n - 1] when the parameter does not extrapolate, and stores
+// the interval j = clamp(floor(xx), -1, n - 1) as the element offset of its
+// coefficient block, 4 (j + 1), beside u = xx - j (GridPoint).
+struct GridDesc {
+  double a, b;
+  int32_t p0;
+  int32_t n;
+  int32_t trunc;
+  int32_t pad;
+};
+static_assert(sizeof(GridDesc) == 32, "GridDesc must stay 32 bytes");
+
+// The interval of one grid at one point: u and the element offset of the
+// coefficient block inside the dial's payload.
+template <typename T>
+struct alignas(sizeof(T) >= 8 ? 16 : 8) GridPoint {
+  T u;
+  int32_t jb;
+};
 
 // A table read by TABULATED / KRIGED dials.
 struct TableDesc {

@@ -28,11 +28,15 @@ class Engine:
         """spline_layout: stored form of the uniform-knot splines, "knots"
         (Catmull-Rom knot values, slopes formed on the device), "slopes"
         (slopes precomputed on the host), "coefs" (per-interval cubic
-        coefficients, extrapolation intervals included) or "auto" (knots for
-        an FP32 engine with k_max == 1, slopes otherwise)."""
+        coefficients, extrapolation intervals included), "grid" (the
+        coefficients with the knot grid shared between splines, its interval
+        formed once per point) or "auto" (knots for an FP32 engine with
+        k_max == 1, grid for k_max >= 32 and for 16 <= k_max < 32 when the
+        grid table holds at most 32 KB, else coefs for an FP64 engine with
+        16 <= k_max < 32, slopes otherwise)."""
         self.lib = N.libgw()
         flags = {"auto": 0, "knots": N.GW_FLAG_SPLINE_KNOTS, "slopes": N.GW_FLAG_SPLINE_SLOPES,
-                 "coefs": N.GW_FLAG_SPLINE_COEFS}[spline_layout]
+                 "coefs": N.GW_FLAG_SPLINE_COEFS, "grid": N.GW_FLAG_SPLINE_GRID}[spline_layout]
         prec = {"fp32": N.GW_FP32, "fp64": N.GW_FP64, "df64": N.GW_DF64}[precision]
         cfg = N.GwConfig(int(n_results), int(n_params), int(n_bins), int(k_max), prec, int(device), int(tile_bytes),
                          flags)

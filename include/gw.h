@@ -74,9 +74,11 @@ enum {
  * with the knot slopes formed in the kernel (fewer bytes per evaluation); or
  * with the slopes precomputed on the host, [low, 1/step, (y, slope) x n]
  * (less arithmetic per evaluation).  No flag: knot values for FP32 engines
- * with k_max == 1 (a bandwidth-bound evaluation), the coefficient form below
- * for FP64 engines with k_max >= 16 (GB300's FP64 rate makes their batched
- * evaluation arithmetic-bound), precomputed slopes otherwise.  Results agree
+ * with k_max == 1 (a bandwidth-bound evaluation), the grid form below for
+ * engines with k_max >= 32 (their batched evaluation is bound by arithmetic
+ * and instruction issue, not bytes) and for engines with 16 <= k_max < 32
+ * whose grid table stays within 32 KB, else the coefficient form for FP64
+ * engines with 16 <= k_max < 32; precomputed slopes otherwise.  Results agree
  * within the precision's rounding; in FP64
  * the per-event weights are identical (the bin sums then differ only in the
  * grouping of their FP64 partial sums, as the tiles are cut differently). */
@@ -91,7 +93,15 @@ enum {
    * slope): one 16-byte load and three multiply-adds per point, about 2.2x
    * the bytes of the slope form.  For batched evaluation, where the
    * arithmetic, not the bytes, bounds the kernel. */
-  GW_FLAG_SPLINE_COEFS = 3
+  GW_FLAG_SPLINE_COEFS = 3,
+  /* The coefficient form with the knot grid shared: monotonic, compact and
+   * uniform splines whose (parameter, first knot, step, knot count) agree
+   * share one grid (up to 16384 grids; splines of further grids keep the
+   * coefficient form), their payload the coefficient blocks alone, and the
+   * interval and fraction of each grid at each point are formed once per
+   * evaluation, beside the parameter mirroring, instead of once per dial.
+   * Per-event weights are identical to the coefficient form's. */
+  GW_FLAG_SPLINE_GRID = 4
 };
 
 /* ---- likelihood evaluated after the histogram step --------------------- */

@@ -124,11 +124,12 @@ def test_bad_config_rejected():
     p = C.c_void_p()
     assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
     assert "bad gw_config" in N.last_error(None)
-    cfg = N.GwConfig(10, 2, 1, 1, 0, 0, 0, 4)  # no such spline form
+    cfg = N.GwConfig(10, 2, 1, 1, 0, 0, 0, 5)  # no such spline form
     assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
     cfg = N.GwConfig(10, 2, 1, 1, 3, 0, 0, 0)  # no such precision
     assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_ERR_ARG
-    for flags in (0, N.GW_FLAG_SPLINE_KNOTS, N.GW_FLAG_SPLINE_SLOPES, N.GW_FLAG_SPLINE_COEFS):
+    for flags in (0, N.GW_FLAG_SPLINE_KNOTS, N.GW_FLAG_SPLINE_SLOPES, N.GW_FLAG_SPLINE_COEFS,
+                  N.GW_FLAG_SPLINE_GRID):
         for prec in (N.GW_FP64, N.GW_FP32, N.GW_DF64):
             cfg = N.GwConfig(10, 2, 1, 1, prec, 0, 0, flags)
             assert lib.gw_create(C.byref(cfg), C.byref(p)) == N.GW_OK

@@ -418,13 +418,16 @@ def test_eigen_decomposed_parameters(c1, c1_oracle):
     e2.close()
 
 
-@pytest.mark.parametrize("prec,layout", [("fp64", "auto"), ("fp32", "auto"), ("df64", "auto"), ("fp32", "coefs")])
+@pytest.mark.parametrize("prec,layout", [("fp64", "auto"), ("fp32", "auto"), ("df64", "auto"), ("fp32", "coefs"),
+                                         ("fp64", "coefs"), ("fp32", "slopes"), ("df64", "slopes")])
 def test_every_compiled_batched_shape(mixed, mixed_oracle, prec, layout):
     """Every compiled batched kernel shape (every family, every register
     target) on the workload with every dial type, K = 64 inflated prior draws
     (extrapolation beyond the knot ranges included), against the oracle; the
     register targets of one shape give identical results.  Also with the
-    uniform-knot splines in the coefficient form."""
+    uniform-knot splines in the grid form (the default at k_max = 64: the
+    coefficients with the knot grid's interval formed once per point), the
+    coefficient form and the slope form."""
     K = 64
     eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021,
                                spline_layout=layout)
@@ -478,7 +481,8 @@ def test_spline_layouts_agree(mixed, mixed_oracle, prec):
     as per-interval cubic coefficients (extrapolation intervals included):
     each within tolerance of the oracle through the K = 1 and the batched
     kernels, with draws far enough out to extrapolate.  In FP64 the knot and
-    slope forms give identical per-event weights; the bin sums differ only in
+    slope forms give identical per-event weights, and so do the coefficient
+    and grid forms in both precisions; the bin sums differ only in
     rounding, because the smaller payload cuts different tiles and so groups
     the FP64 partial sums differently.  The knot form packs fewer bytes, and
     an FP32 K = 1 engine picks it."""
@@ -487,7 +491,7 @@ def test_spline_layouts_agree(mixed, mixed_oracle, prec):
     ref = mixed_oracle.eval(pts)
     tol = (FP64_BIN_REL, FP64_LLH_ABS) if prec == "fp64" else (FP32_BIN_REL, FP32_LLH_ABS)
     out = {}
-    for layout in ("knots", "slopes", "coefs"):
+    for layout in ("knots", "slopes", "coefs", "grid"):
         eng = Engine.from_workload(mixed, precision=prec, k_max=4, llh_type=llh, spline_layout=layout)
         eng.set_event_weight_copy(True)
         weights = []
@@ -501,7 +505,63 @@ def test_spline_layouts_agree(mixed, mixed_oracle, prec):
     if prec == "fp64":
         for wk, ws in zip(out["knots"][0], out["slopes"][0]):
             np.testing.assert_array_equal(wk, ws)
+    # the grid form evaluates the same cubic from the same interval: identical
+    # per-event weights in either precision, four fewer values per spline
+    for wc, wg in zip(out["coefs"][0], out["grid"][0]):
+        np.testing.assert_array_equal(wc, wg)
+    assert out["grid"][1] < out["coefs"][1]
     assert out["knots"][1] < out["slopes"][1]
     auto = Engine.from_workload(mixed, precision=prec, k_max=1, llh_type=llh)
     assert auto.layout()["payload_bytes"] == out["knots" if prec == "fp32" else "slopes"][1]
     auto.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_grid_form_beyond_the_grid_limit(prec):
+    """More distinct knot grids than the grid form holds (16384): the splines
+    of the grids past the limit keep the coefficient form in the same engine.
+    Every spline here has its own step, and three in four share their
+    parameter with others; per-event weights through the K = 1 kernel equal
+    the coefficient form's, and the batched sums agree within rounding."""
+    rng = np.random.default_rng(5)
+    n_ev, P, B = 20000, 50, 40
+    knots = 7
+    types, res, p0, starts, data = [], [], [], [0], []
+    for i in range(n_ev):
+        step = 0.5 + 1e-4 * i  # a grid per spline
+        y = np.exp(np.cumsum(rng.normal(0.0, 0.05, knots)))
+        d = np.concatenate([[-3.0, step], y])
+        for t, pp in ((N.GW_DIAL_MONOTONIC, i % P), (N.GW_DIAL_UNIFORM, (7 * i) % P)):
+            if t == N.GW_DIAL_UNIFORM:
+                d = np.concatenate([[-3.0, step], np.stack([y, rng.normal(0.0, 0.1, knots)], 1).ravel()])
+            types.append(t)
+            res.append(i)
+            p0.append(pp)
+            data.append(d)
+            starts.append(starts[-1] + len(d))
+    bins = rng.integers(0, B, n_ev)
+    pts = rng.normal(0.0, 1.5, (4, P))
+    out = {}
+    for layout in ("coefs", "grid"):
+        e = Engine(n_ev, P, B, k_max=4, precision=prec, spline_layout=layout)
+        e.set_initial_values(np.full(n_ev, 1.0))
+        e.set_event_indices(bins)
+        e.add_dials(np.array(types), np.array(res), np.array(p0), np.full(len(types), -1),
+                    np.array(starts), np.concatenate(data))
+        e.set_data(np.full(B, 500.0))
+        e.set_likelihood(N.GW_LLH_POISSON)
+        e.initialize()
+        e.set_event_weight_copy(True)
+        w = []
+        for k in range(len(pts)):
+            e.eval(pts[k:k + 1])
+            w.append(e.event_weights().copy())
+        out[layout] = (w, e.eval(pts), e.layout()["payload_bytes"])
+        e.close()
+    for a, b in zip(out["coefs"][0], out["grid"][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_allclose(out["grid"][1][0], out["coefs"][1][0], rtol=1e-12 if prec == "fp64" else 1e-6)
+    # 16384 splines lose their four-value prefix, the others keep it
+    tsz = 8 if prec == "fp64" else 4
+    saved = out["coefs"][2] - out["grid"][2]
+    assert 0.9 * 16384 * 4 * tsz <= saved <= 1.1 * 16384 * 4 * tsz + 16 * 2000
