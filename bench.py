@@ -611,7 +611,8 @@ def run_gw(args, world, rank, local, dist):
     if rank == 0 and not args.no_c5 and args.config == "c2":
         from gundam_gb300 import stress
 
-        c5 = stress.run(check_points=2)
+        # progress to stderr: stdout carries the one JSON line
+        c5 = stress.run(check_points=2, log=lambda m: print(m, file=sys.stderr, flush=True))
         c5_check = c5.pop("check", None)
     if rank == 0 and (c1_check or c3_check or c5_check):
         chk = cpu_baseline_checks(c1_check, c3_check, c5_check)

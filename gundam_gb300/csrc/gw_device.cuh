@@ -160,6 +160,33 @@ __device__ __forceinline__ void prepared_values(const T* __restrict__ d, int n, 
   }
 }
 
+// A grid-form dial's inputs at KR points (k0, k0 + kstep, ...): the grid's
+// interval and fraction per point and its response clamp.  The lanes kernel
+// loads them one dial ahead of the evaluation, so the (mostly L2) latency of
+// the grid table overlaps the previous dial's arithmetic.
+template <typename T, int KR>
+struct GridAhead {
+  GridPoint<T> g[KR];
+  typename Vec2<T>::type c;
+};
+
+template <typename T, int KR>
+__device__ __forceinline__ void grid_load(const DevView& v, uint64_t h, int k0, int kstep, GridAhead<T, KR>& a) {
+  const int g = hdr_p0(h);
+  const GridPoint<T>* gp = (const GridPoint<T>*)v.grid_pts + (size_t)g * v.kpad + k0;
+#pragma unroll
+  for (int j = 0; j < KR; ++j) a.g[j] = gp[j * kstep];
+  a.c = ((const typename Vec2<T>::type*)v.grid_clamp)[g];
+}
+
+template <typename T, int KR>
+__device__ __forceinline__ void grid_eval(const T* __restrict__ pl, uint64_t h, const GridAhead<T, KR>& a,
+                                          T (&val)[KR]) {
+  const T* d = pl + hdr_off(h);
+#pragma unroll
+  for (int j = 0; j < KR; ++j) val[j] = clamp_response(coef_cubic(d + a.g[j].jb, a.g[j].u), a.c.x, a.c.y);
+}
+
 // The KR values of one parameter at points k0, k0 + kstep, ...  With VX the
 // points are contiguous (kstep == 1) and k0 * sizeof(T) is a multiple of
 // KR * sizeof(T) (at most 16), so whole 8- or 16-byte vectors are loaded.

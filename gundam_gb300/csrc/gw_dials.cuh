@@ -56,9 +56,12 @@ __device__ __forceinline__ T eval_general(const T* __restrict__ d, int n, T x, b
   }
   const int kc = n - 1;
   int ix = 0;
+  // a step of offset >= kc never moves (ix is still 0 there), so it is
+  // skipped: a branch on the dial's knot count, uniform across a warp in the
+  // lanes-over-points kernels
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    if ((ix + off < kc) && (x > d[3 * (ix + off) + 2])) ix += off;
+    if (off < kc && ix + off < kc && x > d[3 * (ix + off) + 2]) ix += off;
   }
   const T x1 = d[3 * ix + 2];
   const T x2 = d[3 * (ix + 1) + 2];
@@ -82,7 +85,7 @@ __device__ __forceinline__ T eval_graph(const T* __restrict__ d, int n, T x, boo
   int ix = 0;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    if ((ix + off < n) && (x > d[2 * (ix + off) + 1])) ix += off;
+    if (off < n && ix + off < n && x > d[2 * (ix + off) + 1]) ix += off;
   }
   if (ix + 1 >= n) ix--;
   const T p1 = d[2 * ix];

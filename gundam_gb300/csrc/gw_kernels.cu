@@ -509,7 +509,8 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
            (kMaxTileEvents + 1) * sizeof(uint16_t);
   }
   const int nw = b.threads / 32;
-  return (size_t)b.stages * v.tile_payload_bytes + 1024 * sizeof(uint64_t) +
+  // k_batched: headers sized for the engine's largest tile (16-byte multiple)
+  return (size_t)b.stages * v.tile_payload_bytes + (size_t)v.tile_hdr_bytes +
          (size_t)(nw + kMaxLocalBins - 1) * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
          2 * (kMaxTileEvents + 1) * sizeof(uint16_t);
 }

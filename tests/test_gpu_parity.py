@@ -457,6 +457,30 @@ def test_every_compiled_batched_shape(mixed, mixed_oracle, prec, layout):
     eng.close()
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_wide_shapes_at_256_points(mixed, mixed_oracle, prec):
+    """The lanes shapes of 128 points per pass (four points per lane, the
+    grid-form table entries loaded one dial ahead) at K = 256 on the workload
+    with every dial type, grid form (the default at k_max = 256), inflated
+    prior draws: each against the oracle."""
+    K = 256
+    eng = Engine.from_workload(mixed, precision=prec, k_max=K, llh_type=N.GW_LLH_BARLOW_BEESTON_OA2021)
+    pts = mixed.draw_points(K, 78, inflate=2.5)
+    ref = mixed_oracle.eval(pts)
+    tried = 0
+    for i, (kind, ppp, ppt, threads, stages, minb) in enumerate(Engine.compiled_shapes()):
+        if kind != 0 or ppp != 128:
+            continue
+        try:
+            eng.set_shape_index(i)
+        except RuntimeError:
+            continue
+        _check(eng.eval(pts), ref, *_tol(prec), f"shape {(kind, ppp, ppt, threads, stages, minb)}")
+        tried += 1
+    assert tried >= 2
+    eng.close()
+
+
 def test_shape_that_overruns_the_padded_points_is_refused(c1, c1_oracle):
     """K = 150 pads to 192 point columns: a 128-point pass would need 256, so
     the launch is refused with an error (never a read past the arrays); the
