@@ -127,6 +127,41 @@ __device__ __forceinline__ float clamp_response(float r, float lo, float hi) {
   return t;
 }
 
+// A lanes-kernel stage: the tile's payload (TB bytes), its headers in slot
+// order (HB bytes), then its event words, work prefix and base weights, each
+// copied from the 16-byte boundary at or below the tile's first event, so that
+// every input of a tile arrives by bulk copy.  Event buffers hold up to 7
+// leading words of the previous tile and room for the sentinel after the last.
+constexpr int kLaneEvWords = kMaxTileEvents + 8;  // uint16 words per event buffer (528 bytes)
+__host__ __device__ constexpr size_t lanes_ev_bytes(size_t tsz) {
+  return 2 * (size_t)kLaneEvWords * 2 + (((size_t)kMaxTileEvents + 4) * tsz + 15) / 16 * 16;
+}
+
+// Thread 0: every bulk copy of a lanes-kernel tile under one mbarrier.  The
+// event arrays carry 8 words (base weights: 4 values) of slack past their
+// end, so the rounded copies stay inside them.
+// The tile's descriptor goes to *std, where the CTA reads it after its next
+// barrier, so no thread waits on a global load when the tile starts.
+__device__ __forceinline__ void issue_tile_lanes(const DevView& v, int tile, unsigned char* stage, int TB, int HB,
+                                                 uint32_t tsz, uint64_t* bar, TileDesc* std) {
+  const TileDesc td = v.tiles[tile];
+  *std = td;
+  const uint32_t pb = (uint32_t)td.payload_16b * 16u;
+  const uint32_t hb = (((uint32_t)td.ndials + 1u) / 2u) * 16u;
+  const uint32_t e0 = td.event0, ne = td.nevents;
+  const uint32_t a16 = e0 & ~7u;
+  const uint32_t eb = ((e0 - a16 + ne) * 2u + 15u) & ~15u;
+  const uint32_t aw = e0 & ~(16u / tsz - 1u);
+  const uint32_t wb = ((e0 - aw + ne) * tsz + 15u) & ~15u;
+  mbar_expect_tx(bar, pb + hb + 2u * eb + wb);
+  unsigned char* ev = stage + TB + HB;
+  if (pb > 0) bulk_load(stage, v.payload + td.payload_off, pb, bar);
+  if (hb > 0) bulk_load(stage + TB, v.hdr_ev + td.dial0, hb, bar);
+  bulk_load(ev, v.evinfo + a16, eb, bar);
+  bulk_load(ev + 2 * kLaneEvWords, v.evcost + a16, eb, bar);
+  bulk_load(ev + 4 * kLaneEvWords, (const unsigned char*)v.w0 + (size_t)aw * tsz, wb, bar);
+}
+
 // ---------------------------------------------------------------------------
 // One dial at KR parameter points (k0, k0 + kstep, ...): the header is
 // decoded, the type dispatched and the response clamp loaded once; the KR

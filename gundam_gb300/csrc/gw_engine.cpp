@@ -1056,6 +1056,9 @@ int build_and_upload(gw_engine* e) {
   // 6. pack tiles (parallel over tiles)
   std::vector<TileDesc> tdesc((size_t)T_);
   std::vector<uint64_t> hdr((size_t)hdr_total, 0);
+  // the lanes kernel walks a tile's dials event by event: it bulk-copies the
+  // headers in slot order (engines of more than one point)
+  std::vector<uint64_t> hdr_ev(e->cfg.k_max > 1 ? (size_t)hdr_total : 0, 0);
   std::vector<unsigned char> payload((size_t)payload_total, 0);
   std::vector<uint16_t> evinfo((size_t)N);
   std::vector<uint16_t> evcost((size_t)N);
@@ -1109,6 +1112,7 @@ int build_and_upload(gw_engine* e) {
             const int p1 = r.p1 >= 0 ? r.p1 : 0;
             hdr[(size_t)(tp.dial0 + j)] = make_header(g >= 0 ? (int)kGrid : (int)r.type, pn[(size_t)di], slot, off,
                                                       p0, p1);
+            if (!hdr_ev.empty()) hdr_ev[(size_t)(tp.dial0 + slot)] = hdr[(size_t)(tp.dial0 + j)];
             if (r.type == kMonotonic || r.type == kCompact || r.type == kUniform)
               write_prepared<T>(r, e->dial_data.data() + r.data_off, pn[(size_t)di], pl + off,
                                 g >= 0 ? kFormGrid : dial_form);
@@ -1195,6 +1199,11 @@ int build_and_upload(gw_engine* e) {
   v.tiles = (const TileDesc*)p;
   if ((rc = upload(hdr.data(), hdr.size() * sizeof(uint64_t), &p))) return rc;
   v.hdr = (const uint64_t*)p;
+  if (!hdr_ev.empty()) {
+    hdr_ev.resize(hdr_ev.size() + 2, 0);
+    if ((rc = upload(hdr_ev.data(), hdr_ev.size() * sizeof(uint64_t), &p))) return rc;
+    v.hdr_ev = (const uint64_t*)p;
+  }
   if ((rc = upload(payload.data(), payload.size(), &p))) return rc;
   v.payload = (const unsigned char*)p;
   if ((rc = upload(evinfo.data(), evinfo.size() * sizeof(uint16_t), &p))) return rc;

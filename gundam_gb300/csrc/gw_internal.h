@@ -36,6 +36,7 @@ struct DevView {
 
   const TileDesc* tiles;
   const uint64_t* hdr;
+  const uint64_t* hdr_ev;     // the same headers, each tile's in slot (event-major) order (engines with k_max > 1)
   const unsigned char* payload;
   const uint16_t* evinfo;
   const uint16_t* evcost;     // [n_events] summed dial_cost + kEventCost through the event, from its tile's first

@@ -509,10 +509,10 @@ size_t batched_smem_bytes(const DevView& v, const BatchedShape& b) {
            (kMaxTileEvents + 1) * sizeof(uint16_t);
   }
   const int nw = b.threads / 32;
-  // k_batched: headers sized for the engine's largest tile (16-byte multiple)
-  return (size_t)b.stages * v.tile_payload_bytes + (size_t)v.tile_hdr_bytes +
-         (size_t)(nw + kMaxLocalBins - 1) * b.kr * 32 * sizeof(double2) + kMaxTileEvents * tsz +
-         2 * (kMaxTileEvents + 1) * sizeof(uint16_t);
+  // k_batched: per stage the payload, the headers (sized for the engine's
+  // largest tile) and the event buffers; then the bin partials
+  return (size_t)b.stages * ((size_t)v.tile_payload_bytes + (size_t)v.tile_hdr_bytes + lanes_ev_bytes(tsz)) +
+         (size_t)(nw + kMaxLocalBins - 1) * b.kr * 32 * sizeof(double2);
 }
 
 template <typename T>

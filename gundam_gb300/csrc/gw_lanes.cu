@@ -26,51 +26,47 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
   constexpr int NE = NW + kMaxLocalBins - 1;
   extern __shared__ __align__(128) unsigned char smem[];
   const int TB = v.tile_payload_bytes;
-  unsigned char* stage0 = smem;
-  unsigned char* stage1 = smem + (ST == 2 ? TB : 0);
-  uint64_t* shdr = (uint64_t*)(smem + ST * TB);               // [tile_hdr_bytes / 8], indexed by slot
-  double2* wpart = (double2*)(smem + ST * TB + v.tile_hdr_bytes);  // [NE][KR][32]
-  T* sw0 = (T*)(wpart + NE * KR * 32);                        // [256]
-  uint16_t* sev = (uint16_t*)(sw0 + kMaxTileEvents);          // [257]
-  uint16_t* sec = sev + (kMaxTileEvents + 1);                 // [257]: work before each event, total last
+  const int HB = v.tile_hdr_bytes;
+  // ST stages of [payload | headers in slot order | event words | work
+  // prefix | base weights], every part filled by bulk copy (issue_tile_lanes)
+  const int SB = TB + HB + (int)lanes_ev_bytes(sizeof(T));
+  double2* wpart = (double2*)(smem + ST * SB);               // [NE][KR][32]
   __shared__ uint64_t bar[2];
+  __shared__ TileDesc s_td[2];
   __shared__ int s_present[kMaxLocalBins];
   __shared__ int s_run[NW][2];  // first, last local bin of each warp's run (first > last: none)
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
+  int tile = blockIdx.x;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
+    if (tile < v.n_tiles) issue_tile_lanes(v, tile, smem, TB, HB, sizeof(T), &bar[0], &s_td[0]);
   }
   __syncthreads();
 
-  int tile = blockIdx.x;
-  if (tid == 0 && tile < v.n_tiles) issue_tile(v, tile, stage0, &bar[0]);
   for (int it = 0; tile < v.n_tiles; ++it, tile += gridDim.x) {
     const int st = (ST == 2) ? (it & 1) : 0;
     const uint32_t parity = (ST == 2) ? (uint32_t)((it >> 1) & 1) : (uint32_t)(it & 1);
     const int next = tile + gridDim.x;
-    if (ST == 2 && tid == 0 && next < v.n_tiles) issue_tile(v, next, st ? stage0 : stage1, &bar[st ^ 1]);
+    const TileDesc td = s_td[st];
+    if (ST == 2 && tid == 0 && next < v.n_tiles)
+      issue_tile_lanes(v, next, smem + (st ^ 1) * SB, TB, HB, sizeof(T), &bar[st ^ 1], &s_td[st ^ 1]);
 
-    const TileDesc td = v.tiles[tile];
     const int nd = td.ndials, ne = td.nevents;
-    for (int i = tid; i < nd; i += NT) {
-      const uint64_t h = v.hdr[td.dial0 + i];
-      shdr[hdr_slot(h)] = h;
-    }
-    for (int e = tid; e < ne; e += NT) {
-      sev[e] = v.evinfo[td.event0 + e];
-      sec[e + 1] = v.evcost[td.event0 + e];
-      sw0[e] = ((const T*)v.w0)[td.event0 + e];
-    }
-    if (tid == 0) {
-      sev[ne] = make_evinfo(nd, 0);
-      sec[0] = 0;
-    }
+    unsigned char* stage = smem + st * SB;
+    const uint64_t* shdr = (const uint64_t*)(stage + TB);  // indexed by slot
+    unsigned char* evb = stage + TB + HB;
+    // sev[e]: event e's first slot and local bin, sev[ne] the sentinel;
+    // secc[e]: estimated work through event e; sw0[e]: its base weight
+    uint16_t* sev = (uint16_t*)evb + (td.event0 & 7u);
+    const uint16_t* secc = (const uint16_t*)(evb + 2 * kLaneEvWords) + (td.event0 & 7u);
+    const T* sw0 = (const T*)(evb + 4 * kLaneEvWords) + (td.event0 & (16u / sizeof(T) - 1u));
     if (tid < kMaxLocalBins) s_present[tid] = 0;
     const bool ok = mbar_wait_bounded(&bar[st], parity, kWaitLimitNs);
+    if (tid == 0 && ok) sev[ne] = make_evinfo(nd, 0);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         atomicOr(v.status, kStatusCopyTimeout);
@@ -83,22 +79,23 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
       return;
     }
     for (int e = tid; e < ne; e += NT) s_present[ev_lbin(sev[e])] = 1;
-    const T* pl = (const T*)(st ? stage1 : stage0);
+    const T* pl = (const T*)stage;
 
     // Each warp takes a contiguous run of events holding ~1/NW of the tile's
     // estimated work (dial_cost): the first event whose preceding work
     // reaches warp*total/NW (a fixed, deterministic split, so the FP64
     // summation order does not depend on scheduling).
+    auto before = [&](int e) { return e == 0 ? 0 : (int)secc[e - 1]; };  // work before event e
     auto first_event_at = [&](int target) {
-      int lo = 0, hi = ne;  // sec[ne] holds the total
+      int lo = 0, hi = ne;  // before(ne) is the total
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if ((int)sec[mid] < target) lo = mid + 1;
+        if (before(mid) < target) lo = mid + 1;
         else hi = mid;
       }
       return lo;
     };
-    const int total = sec[ne];
+    const int total = before(ne);
     const int e_lo = (warp == 0) ? 0 : first_event_at((warp * total) / NW);
     const int e_hi = (warp == NW - 1) ? ne : first_event_at(((warp + 1) * total) / NW);
     const int b_first = (e_lo < e_hi) ? ev_lbin(sev[e_lo]) : 1;
@@ -215,7 +212,8 @@ __global__ void __launch_bounds__(NT, MB) k_batched(const DevView v, int K) {
       __syncthreads();
       // one stage: after the last pass nothing reads the payload any more, so
       // the next tile's copy overlaps this tile's reduction
-      if (ST == 1 && kb + KP >= K && tid == 0 && next < v.n_tiles) issue_tile(v, next, stage0, &bar[0]);
+      if (ST == 1 && kb + KP >= K && tid == 0 && next < v.n_tiles)
+        issue_tile_lanes(v, next, smem, TB, HB, sizeof(T), &bar[0], &s_td[0]);
       for (int t = tid; t < kMaxLocalBins * KP; t += NT) {
         const int lb = t / KP, r = t % KP;
         const int j = r / KC, kk = r % KC;
