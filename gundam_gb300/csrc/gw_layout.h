@@ -92,6 +92,7 @@ GW_HD int dial_cost(int type, int n) {
   }
 }
 constexpr int kEventCost = 10;
+static_assert(kMaxTileDials * 40 + kMaxTileEvents * kEventCost < 65536, "a tile's work must fit 16 bits");
 
 // 16-bit per-event word: [0,10) first slot of the event, [10,13) local bin.
 GW_HD uint16_t make_evinfo(int slot0, int lbin) {
