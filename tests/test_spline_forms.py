@@ -10,7 +10,10 @@ points at a time in packed FP32 with the cubic rearranged (`eval_prepared2`).
 These checks pin the arithmetic of those forms on the CPU: the slope rule and
 its end-knot cases, the interval and extrapolation rules, and the rearranged
 Hermite cubic, in FP64 (to 1e-12 of the knot scale) and in FP32 arithmetic
-(to 2e-5).  The GPU parity tests run the compiled kernels.
+(to 2e-5).  The same for the per-interval coefficient blocks that the
+coefficient and grid forms store (Catmull-Rom and uniform splines, the
+extrapolation blocks re-expanded about their own origin).  The GPU parity
+tests run the compiled kernels.
 """
 import math
 
@@ -146,5 +149,95 @@ def test_stored_forms_in_fp32_arithmetic(form):
         for x in xs:
             ref = O.dial(MONOTONIC, np.concatenate([[low, step], y]), float(f(x)), 0.0, False)
             got = float(evaluate(form, f(low), f(1.0 / step), y.astype(f), s.astype(f), f(x), False, True, f))
+            worst = max(worst, abs(got - ref) / max(abs(ref), scale))
+    assert worst <= 2e-5, worst
+
+
+# ---------------------------------------------------------------------------
+# The coefficient form (GW_FLAG_SPLINE_COEFS) and the grid form
+# (GW_FLAG_SPLINE_GRID), which evaluates the same blocks from an interval and
+# fraction formed once per knot grid: write_prepared's per-interval cubics,
+# the two extrapolation blocks re-expanded about their own origin, and
+# coef_interval + the Horner cubic of eval_coef / the grid path.
+# ---------------------------------------------------------------------------
+UNIFORM = 3
+
+
+def coef_blocks(y, sl, catmull):
+    """write_prepared (coefficient / grid form): block j + 1 holds the cubic of
+    u = xx - j on interval j; blocks 0 and n the extrapolation beyond the ends."""
+    n = len(y)
+
+    def cubic(i, m1, m2):
+        dc = y[i + 1] - y[i]
+        return [y[i], m1, 3.0 * dc - 2.0 * m1 - m2, m1 + m2 - 2.0 * dc]
+
+    blocks = [None] * (n + 1)
+    for j in range(n - 1):
+        blocks[j + 1] = cubic(j, sl[j], sl[j + 1])
+    c = cubic(0, sl[0], (y[1] - y[0]) if catmull else sl[1])
+    blocks[0] = [c[0] - c[1] + c[2] - c[3], c[1] - 2.0 * c[2] + 3.0 * c[3], c[2] - 3.0 * c[3], c[3]]
+    c = cubic(n - 2, (y[n - 1] - y[n - 2]) if catmull else sl[n - 2], sl[n - 1])
+    blocks[n] = [c[0] + c[1] + c[2] + c[3], c[1] + 2.0 * c[2] + 3.0 * c[3], c[2] + 3.0 * c[3], c[3]]
+    return blocks
+
+
+def eval_coef(blocks, low, step, x, trunc, f):
+    """coef_interval + coef_cubic: xx = x b + a, the truncation clamp,
+    j = clamp(floor(xx), -1, n - 1), u = xx - j, block j + 1 at u."""
+    n = len(blocks) - 1
+    xx = f(x) * f(1.0 / step) + f(-low / step)
+    if trunc:
+        xx = min(max(xx, f(0)), f(n - 1))
+    fj = min(max(f(math.floor(xx)), f(-1)), f(n - 1))
+    u = xx - fj
+    c = [f(q) for q in blocks[int(fj) + 1]]
+    return c[0] + u * (c[1] + u * (c[2] + u * c[3]))
+
+
+def uniform_cases(seed, count):
+    rng = np.random.default_rng(seed)
+    for low, step, y, xs in cases(seed, count):
+        yield low, step, y, rng.normal(0.0, 0.5, len(y)), xs
+
+
+@pytest.mark.parametrize("dial_type", [MONOTONIC, COMPACT, UNIFORM])
+def test_coefficient_form_matches_the_reference_in_fp64(dial_type):
+    """Within two knot steps of the range the re-expanded blocks reproduce the
+    reference to 1e-12 of the knot scale; further out the extrapolated cubic
+    grows as u^3 and the bound is taken on the value itself."""
+    limit = dial_type == MONOTONIC
+    worst = 0.0
+    for low, step, y, dydx, xs in uniform_cases(211 + dial_type, 150):
+        n = len(y)
+        if dial_type == UNIFORM:
+            data = np.concatenate([[low, step], np.stack([y, dydx], 1).ravel()])
+            sl = dydx * step
+        else:
+            data = np.concatenate([[low, step], y])
+            sl = host_slopes(y, limit)
+        blocks = coef_blocks(y, sl, dial_type != UNIFORM)
+        scale = max(1.0, float(np.max(np.abs(y))))
+        for trunc in (False, True):
+            for x in xs:
+                ref = O.dial(dial_type, data, float(x), 0.0, trunc)
+                got = eval_coef(blocks, low, step, float(x), trunc, float)
+                near = low - 2 * step <= x <= low + (n + 1) * step
+                worst = max(worst, abs(got - ref) / (max(abs(ref), scale) if near else max(abs(ref), 1.0)))
+    assert worst <= 1e-12, worst
+
+
+def test_coefficient_form_in_fp32_arithmetic():
+    """FP32 blocks and interval within one knot step of the range, as the
+    engine's FP32 mode evaluates them (the same bar as the other forms)."""
+    f = np.float32
+    worst = 0.0
+    for low, step, y, xs in cases(307, 120):
+        blocks = coef_blocks(y, host_slopes(y, True), True)
+        scale = max(1.0, float(np.max(np.abs(y))))
+        xs = np.clip(xs, low - step, low + len(y) * step)
+        for x in xs:
+            ref = O.dial(MONOTONIC, np.concatenate([[low, step], y]), float(f(x)), 0.0, False)
+            got = float(eval_coef(blocks, low, step, f(x), False, f))
             worst = max(worst, abs(got - ref) / max(abs(ref), scale))
     assert worst <= 2e-5, worst
