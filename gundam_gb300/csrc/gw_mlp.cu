@@ -868,8 +868,9 @@ static int gwm_alloc(gwm_net* n, T** p, size_t count) {
   return GW_OK;
 }
 
-constexpr int kStages = 4;
-static size_t gemm_smem(int bn) { return (size_t)kStages * (gwm::kBM * gwm::kBK * 2 + bn * gwm::kBK * 2) + 1024; }
+static size_t gemm_smem(int bn, int stages) {
+  return (size_t)stages * (gwm::kBM * gwm::kBK * 2 + bn * gwm::kBK * 2) + 1024;
+}
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -908,31 +909,39 @@ static int make_map(gwm_net* n, CUtensorMap* map, const bf16* p, int rows, int K
   return GW_OK;
 }
 
-template <int BN>
+template <int BN, int S>
 static int launch_gemm(gwm_net* n, const bf16* A, const bf16* B, int M, int N, int K, const gwm::Epilogue& ep) {
   CUtensorMap ma, mb;
   int rc = make_map(n, &ma, A, M, K, gwm::kBM);
   if (!rc) rc = make_map(n, &mb, B, N, K, BN);
   if (rc) return rc;
-  const size_t smem = gemm_smem(BN);
+  const size_t smem = gemm_smem(BN, S);
   static std::once_flag once;
   std::call_once(once, [smem]() {
-    cudaFuncSetAttribute(gwm::k_gemm<BN, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(gwm::k_gemm<BN, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   dim3 grid((N + BN - 1) / BN, (M + gwm::kBM - 1) / gwm::kBM);
-  gwm::k_gemm<BN, kStages><<<grid, gwm::kThreads, smem, n->stream>>>(ma, mb, M, N, K, ep, n->status);
+  gwm::k_gemm<BN, S><<<grid, gwm::kThreads, smem, n->stream>>>(ma, mb, M, N, K, ep, n->status);
   GWM_CUDA(n, cudaGetLastError());
   return GW_OK;
 }
 
-// C[M x N] = A[M x K] * B[N x K]^T with the given epilogue.  Small M takes
-// narrow tiles so that more CTAs share the K loop.
+// C[M x N] = A[M x K] * B[N x K]^T with the given epilogue.  The widest tile
+// that still gives one CTA per SM or more (148 of GB300's 152), else the
+// narrowest (64 columns): at the network's sizes a launch is one wave, and
+// a tile runs few K steps, so more CTAs, not wider tiles, keep the tensor
+// pipe busy (hidden layers, M = 2048, N = 512: 64 CTAs of 128 columns left
+// 88 SMs idle).  Ring depth: 128 x 256 tiles take two stages, so that two CTAs
+// (and their accumulators, 256 TMEM columns each) share an SM and one's
+// epilogue overlaps the other's MMAs; 64- and 128-column tiles take four.
+// The tile shape does not change the order of any accumulation.
 static int gemm(gwm_net* n, const bf16* A, const bf16* B, int M, int N, int K, const gwm::Epilogue& ep) {
   if (K % 8 != 0) return gwm_fail(n, GW_ERR_ARG, "GEMM K must be a multiple of 8");
   const int tiles_m = (M + gwm::kBM - 1) / gwm::kBM;
-  if (N <= 64 || tiles_m * ((N + 127) / 128) < 64) return launch_gemm<64>(n, A, B, M, N, K, ep);
-  if (N <= 128 || tiles_m * ((N + 255) / 256) < 64) return launch_gemm<128>(n, A, B, M, N, K, ep);
-  return launch_gemm<256>(n, A, B, M, N, K, ep);
+  constexpr int kWave = 148;
+  if (N > 128 && tiles_m * ((N + 255) / 256) >= kWave) return launch_gemm<256, 2>(n, A, B, M, N, K, ep);
+  if (N > 64 && tiles_m * ((N + 127) / 128) >= kWave) return launch_gemm<128, 4>(n, A, B, M, N, K, ep);
+  return launch_gemm<64, 4>(n, A, B, M, N, K, ep);
 }
 
 static int check_status(gwm_net* n) {
