@@ -141,11 +141,15 @@ __host__ __device__ constexpr size_t lanes_ev_bytes(size_t tsz) {
 // event arrays carry 8 words (base weights: 4 values) of slack past their
 // end, so the rounded copies stay inside them.
 // The tile's descriptor goes to *std, where the CTA reads it after its next
-// barrier, so no thread waits on a global load when the tile starts.
+// barrier, so no thread waits on a global load when the tile starts.  The
+// calling thread writes a sentinel into the stage's event words after each
+// copy lands; the proxy fence orders that write before the bulk copies that
+// overwrite the stage next.
 __device__ __forceinline__ void issue_tile_lanes(const DevView& v, int tile, unsigned char* stage, int TB, int HB,
                                                  uint32_t tsz, uint64_t* bar, TileDesc* std) {
   const TileDesc td = v.tiles[tile];
   *std = td;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   const uint32_t pb = (uint32_t)td.payload_16b * 16u;
   const uint32_t hb = (((uint32_t)td.ndials + 1u) / 2u) * 16u;
   const uint32_t e0 = td.event0, ne = td.nevents;
