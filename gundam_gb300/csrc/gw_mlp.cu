@@ -186,12 +186,18 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const __grid_constant__ CUten
   constexpr int kB = BN * kBK * 2;
   constexpr int kStage = kA + kB;
   __shared__ __align__(8) uint64_t full[S], empty[S], done;
+  __shared__ float sbias[BN];  // the tile's bias columns, read by every row of the epilogue
   __shared__ uint32_t tmem_base;
   __shared__ volatile int failed;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
   if (warp == 0) tmem_alloc(&tmem_base, BN);
+  if (ep.bias) {
+    // one coalesced load per column instead of one load per element in the
+    // epilogue, where the dependent loads stalled the tile's four warps
+    for (int c = tid; c < BN; c += kThreads) sbias[c] = (n0 + c < N) ? ep.bias[n0 + c] : 0.f;
+  }
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
       mbar_init(&full[i], 1);
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm(const __grid_constant__ CUten
     }
 #pragma unroll
     for (int q = 0; q < 32; ++q)
-      if (ep.bias && q < ncol) v[q] += ep.bias[n0 + c0 + q];
+      if (ep.bias && q < ncol) v[q] += sbias[c0 + q];
     if (ep.out_f32) {
       __syncwarp();
 #pragma unroll
